@@ -1,0 +1,359 @@
+"""Benchmark of the ray-integration hot path on GB300.
+
+Workload (default): the plain FP64 drop-in case -- 65,536 rays over a
+2,001 x 2,001 seamount grid at 50 m with a uniform (0.5, 0) m/s current grid,
+dt = 1 s, 4,000 RK4 steps, full trajectories (10.5 GB per step).  One bench
+step = one trace call over all rays.  Metric: ray-steps/s (one ray-step = one
+RK4 step = four right-hand-side evaluations).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Under torchrun each rank traces its own copy of the workload (rays are
+independent, no collective; weak scaling) and rank 0 prints one JSON line.
+`--impl reference` times the CPU restatement of the reference path on the
+host cores instead (rank 0 only).
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "ray-steps/s"
+L2_FLUSH_BYTES = 512 << 20  # > 129 MB L2
+
+# Algorithmic work of one ray-step of the plain FP64 form over f64 grids:
+# 4 stages x 3 fields (h, u, v) x 4 corners x 8 B of grid gathers, plus one
+# stored 40 B output row (t, x, y, kx, ky).
+GRID_BYTES_PER_RAY_STEP = 4 * 3 * 4 * 8
+OUT_BYTES_PER_ROW = 5 * 8
+# FP64 floating-point operations one ray-step executes (DADD/DMUL = 1,
+# DFMA = 2), counted by ncu on the plain kernel over the seamount workload
+# (sm__sass_thread_inst_executed_op_d{add,mul,fma}_pred_on; profiles/).
+FP64_FLOP_PER_RAY_STEP = None
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--rays", type=int, default=65536)
+    p.add_argument("--trace-steps", type=int, default=4000)
+    p.add_argument("--cpu-seconds", type=float, default=12.0,
+                   help="wall-time budget of the CPU-baseline sample")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def cpu_threads() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:  # pragma: no cover
+        return os.cpu_count() or 1
+
+
+def cpu_sample(w, seconds: float, threads: int):
+    """Times the oracle (CPU restatement of the reference path, OpenMP over
+    rays) on successive batches of the workload's rays until `seconds` pass.
+    Returns (ray-steps/s, description)."""
+    from oracle import pyoracle
+
+    ob = pyoracle.Bathymetry.grid(w.bx, w.by, w.depth)
+    oc = pyoracle.Current.grid(w.cx, w.cy, w.u, w.v)
+    batch = max(threads * 16, 256)
+    done_rays = 0
+    ray_steps = 0
+    t_start = time.perf_counter()
+    i = 0
+    while True:
+        idx = np.arange(i, i + batch) % w.n
+        traj, n_rows, _ = pyoracle.trace(ob, oc, w.x0[idx], w.y0[idx], w.kx0[idx], w.ky0[idx],
+                                         w.t0, w.t_end, w.dt, threads=threads)
+        ray_steps += int(np.sum(n_rows.astype(np.int64) - 1))
+        done_rays += batch
+        i += batch
+        elapsed = time.perf_counter() - t_start
+        if elapsed >= seconds:
+            break
+    desc = (f"{done_rays} of the workload's rays (batches of {batch}) x up to "
+            f"{int(round((w.t_end - w.t0) / w.dt))} steps with full trajectories, "
+            f"{threads} OpenMP threads, {elapsed:.1f} s wall")
+    return ray_steps / elapsed, desc, elapsed
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": smax, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def reference_arm(args, rank: int, world: int):
+    """The reference's CPU path (the oracle port: the Rust crate cannot be
+    built here) on the host cores, each step a bounded sample."""
+    if rank != 0:
+        return
+    from mantaray_gb300.workloads import seamount
+
+    w = seamount(n_rays=args.rays, steps=args.trace_steps)
+    threads = cpu_threads()
+    per_step = max(args.cpu_seconds / 4.0, 1.0)
+    for _ in range(args.warmup):
+        cpu_sample(w, per_step / 4.0, threads)
+    rates, descs, times = [], [], []
+    for _ in range(args.steps):
+        r, d, t = cpu_sample(w, per_step, threads)
+        rates.append(r)
+        descs.append(d)
+        times.append(t)
+    value = statistics.mean(rates)
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "impl": "reference",
+        "config": {"workload": w.name, "rays": w.n, "grid": "2001x2001 f64", "dt": w.dt,
+                   "parallelism": "host threads"},
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
+                         "sample": descs[-1]},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def gb300_arm(args, rank: int, world: int, local_rank: int):
+    import torch
+
+    import mantaray_gb300 as mr
+    from mantaray_gb300.workloads import seamount
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist  # noqa: F811
+
+        dist.init_process_group("nccl", device_id=dev)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    w = seamount(n_rays=args.rays, steps=args.trace_steps)
+    b = mr.Bathymetry.grid(w.bx, w.by, w.depth)
+    c = mr.Current.grid(w.cx, w.cy, w.u, w.v)
+    rows = mr.num_steps(w.t0, w.t_end, w.dt) + 1
+    n = w.n
+    ins = [torch.from_numpy(a).to(dev) for a in (w.x0, w.y0, w.kx0, w.ky0)]
+    traj = torch.empty((5, rows, n), dtype=torch.float64, device=dev)
+    n_rows = torch.empty(n, dtype=torch.int32, device=dev)
+    status = torch.empty(n, dtype=torch.uint8, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def one():
+        mr.trace_device(b, c, *ins, w.t0, w.t_end, w.dt, traj, n_rows, status, stream=stream)
+
+    for _ in range(args.warmup):
+        one()
+    torch.cuda.synchronize()
+
+    # ---- device-resident throughput (value) ----
+    times = []
+    launches = 0
+    with ClockSampler(local_rank) as clocks:
+        barrier()
+        torch.cuda.synchronize()
+        for _ in range(args.steps):
+            flush.fill_(1.0)  # evict L2 between timed steps (not timed)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            one()
+            e1.record(stream)
+            launches += 1
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+        torch.cuda.synchronize()
+        barrier()
+    clock = clocks.summary()
+    ray_steps = int(torch.sum(n_rows.to(torch.int64) - 1).item())
+    local_t = sum(times)
+    t_max = local_t
+    if dist is not None:
+        tt = torch.tensor([local_t], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max = float(tt.item())
+    total_ray_steps = ray_steps * args.steps * world
+    value = total_ray_steps / t_max
+    kernel_s = local_t / args.steps
+
+    # ---- end-to-end through the C ABI with host buffers (e2e) ----
+    e2e = None
+    if not args.no_e2e:
+        hin = [torch.from_numpy(a.copy()).pin_memory() for a in (w.x0, w.y0, w.kx0, w.ky0)]
+        hout = torch.empty((5, rows, n), dtype=torch.float64, pin_memory=True)
+        hout_np = hout.numpy()
+        h_np = [t.numpy() for t in hin]
+        mr.trace(b, c, *h_np, w.t_end - w.t0, w.dt, t0=w.t0, out=hout_np)  # warm-up
+        barrier()
+        e2e_times = []
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            res = mr.trace(b, c, *h_np, w.t_end - w.t0, w.dt, t0=w.t0, out=hout_np)
+            e2e_times.append(time.perf_counter() - t0)
+        barrier()
+        e2e_local = sum(e2e_times)
+        e2e_max = e2e_local
+        if dist is not None:
+            tt = torch.tensor([e2e_local], device=dev)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            e2e_max = float(tt.item())
+        e2e_steps = int(np.sum(res.n_rows.astype(np.int64) - 1))
+        e2e = {"value": e2e_steps * args.steps * world / e2e_max, "unit": METRIC,
+               "h2d_bytes_per_step": 4 * n * 8,
+               "d2h_bytes_per_step": 5 * rows * n * 8 + n * 4 + n,
+               "path": "mr_trace (C ABI), page-locked host buffers; the kernel stores "
+                       "trajectories straight into host memory",
+               "ms_per_step": 1e3 * e2e_local / args.steps}
+        del hout, hin
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+
+    # ---- roofline of the dominant kernel (rk4_f64) ----
+    L = mr._native.load()
+    import ctypes
+
+    fp64_peak = ctypes.c_double()
+    mr._native.check(L.mr_measure_fma_peak(1, ctypes.byref(fp64_peak)))
+    rs_per_s_kernel = ray_steps / kernel_s
+    hbm_achieved = rs_per_s_kernel * (GRID_BYTES_PER_RAY_STEP + OUT_BYTES_PER_ROW) / 1e9
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    if FP64_FLOP_PER_RAY_STEP:
+        fp64_achieved = rs_per_s_kernel * FP64_FLOP_PER_RAY_STEP / 1e12
+        roofline = {"bound": "fp64", "achieved": fp64_achieved, "peak": fp64_peak.value,
+                    "unit": "TFLOP/s", "frac": fp64_achieved / fp64_peak.value,
+                    "peak_source": "measured: FP64 FMA-chain kernel on this GPU, this run",
+                    "flop_per_ray_step": FP64_FLOP_PER_RAY_STEP}
+    else:
+        roofline = {"bound": "fp64", "achieved": None, "peak": fp64_peak.value,
+                    "unit": "TFLOP/s", "frac": None,
+                    "peak_source": "measured: FP64 FMA-chain kernel on this GPU, this run"}
+    roofline["hbm"] = {"achieved": hbm_achieved, "peak": hbm_peak, "unit": "GB/s",
+                       "frac": hbm_achieved / hbm_peak,
+                       "bytes_per_ray_step": GRID_BYTES_PER_RAY_STEP + OUT_BYTES_PER_ROW,
+                       "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"}
+    roofline["traffic"] = None
+    roofline["kernel_ms"] = 1e3 * kernel_s
+
+    cpu = None
+    if not args.no_cpu_baseline:
+        threads = cpu_threads()
+        rate, desc, _ = cpu_sample(w, args.cpu_seconds, threads)
+        cpu = {"value": rate, "unit": METRIC, "cores": threads, "kind": "port", "sample": desc}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": w.name, "form": "plain FP64 (rk4_f64), one launch per call",
+                   "rays_per_gpu": n, "steps_per_ray": rows - 1, "grid": "2001x2001 f64 depth/u/v",
+                   "dt": w.dt, "stop_rule": "stage1",
+                   "l2": "512 MB buffer written between timed steps; each step also writes 10.5 GB",
+                   "parallelism": f"replicas x{world}"},
+        "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+        "clocks": clock,
+    }
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", args.gpus if "RANK" in os.environ else 1))
+    local_rank = int(os.environ.get("LOCAL_RANK", 0))
+    if args.impl == "reference":
+        reference_arm(args, rank, world)
+    else:
+        gb300_arm(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    main()

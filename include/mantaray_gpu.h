@@ -1,0 +1,199 @@
+/*
+ * mantaray_gpu.h -- C ABI of the GB300 ray-integration library
+ * (libmantaray_gpu.so).
+ *
+ * Drop-in boundary for the hot path of mines-oceanography/mantaray: the Rust
+ * extension module `_mantaray` (src/ffi.rs:18-85) and the drivers beneath it
+ * (ManyRays::trace_many, src/ray.rs:98-127; SingleRay::trace_individual,
+ * src/ray.rs:198-213) over the field types of src/bathymetry/ and
+ * src/current/.  Plain pointers and sizes only.
+ *
+ * Conventions
+ *  - Every function returns MR_OK (0) or a negative MR_ERR_* code; the
+ *    message of the last failure on the calling thread is mr_last_error().
+ *  - Field handles own device (HBM) copies of their grids, made once at
+ *    creation on the device current at that time, and are immutable: one
+ *    handle may serve any number of concurrent trace calls.
+ *  - Trajectories are stored traj[5][rows_cap][n] (f64; variables t, x, y,
+ *    kx, ky; time-major, ray fastest): the (time_step, ray) layout of the
+ *    reference's xarray result (python/mantaray/core.py:114-125).  Rows past
+ *    a ray's last row are NaN (core.py:116-119 pads with NaN).
+ *  - n_rows[i] counts the rows the reference records for ray i: the initial
+ *    state plus one row per step taken, the last one included when the stop
+ *    rule ends the ray (src/wave_ray_path.rs:600-626).
+ *  - Per-ray failures do not fail the call: the reference turns every RHS
+ *    error into NaN (src/wave_ray_path.rs:220-234) and stops the ray;
+ *    status[i] says which way each ray ended.
+ */
+#ifndef MANTARAY_GPU_H
+#define MANTARAY_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- return codes ------------------------------------------------------ */
+#define MR_OK 0
+/* An argument is invalid (null pointer, size mismatch, axis with fewer than
+ * two points, unknown option).  Error::InvalidArgument, src/error.rs:12-14. */
+#define MR_ERR_INVALID_ARGUMENT (-1)
+/* A CUDA runtime call failed (message names the call). */
+#define MR_ERR_CUDA (-2)
+/* A file could not be opened or read.  Error::IOError, src/error.rs:26-28;
+ * the reference panics here (src/ffi.rs:36-38). */
+#define MR_ERR_IO (-3)
+/* Not a NetCDF-3 classic/64-bit-offset file, or a variable is missing.
+ * Error::ReadError, src/error.rs:34-36. */
+#define MR_ERR_READ (-4)
+/* rows_cap < mr_num_steps(t0, t_end, dt) + 1. */
+#define MR_ERR_CAPACITY (-5)
+/* Device or host allocation failed. */
+#define MR_ERR_OUT_OF_MEMORY (-6)
+
+/* ---- per-ray status ------------------------------------------------------ */
+#define MR_RAY_COMPLETE 0 /* all ceil((t_end - t0)/dt) steps taken */
+#define MR_RAY_STOPPED 1  /* ended by the solout rule (src/wave_ray_path.rs:236-246) */
+
+/* ---- stop rule ----------------------------------------------------------
+ * Which derivative the solout test sees after each step.  The stepper crate
+ * (ode_solvers 0.4.0) is not in the reference tree, so both readings are
+ * offered; they differ only by whether a ray whose new state is finite but
+ * out of the domain records one more, all-NaN, row.
+ *   MR_STOP_STAGE1: the first-stage derivative of the step just taken.
+ *   MR_STOP_FRESH:  the derivative evaluated at the new state. */
+#define MR_STOP_STAGE1 0
+#define MR_STOP_FRESH 1
+
+typedef struct mr_bathymetry mr_bathymetry;
+typedef struct mr_current mr_current;
+
+/* ---- bathymetry ---------------------------------------------------------- */
+
+/* Gridded bathymetry (replaces CartesianNetcdf3, src/bathymetry/
+ * cartesian_netcdf3.rs:35-43 and :167-256): f32 axes x[nx], y[ny], f64 depth
+ * of depth_len values read with flat index nx*j + i (:465-471).  depth_len
+ * may differ from nx*ny exactly as in the reference (lookups past the end
+ * become IndexOutOfBounds, i.e. NaN).  nx, ny >= 2 (the reference panics on
+ * a one-point axis at its first lookup). */
+int mr_bathymetry_grid(size_t nx, size_t ny, const float *x, const float *y,
+                       const double *depth, size_t depth_len,
+                       mr_bathymetry **out);
+
+/* CartesianNetcdf3::open(path, x_name, y_name, depth_name)
+ * (cartesian_netcdf3.rs:167-256): reads a NetCDF-3 file; i8/u8/i16/i32/f32/
+ * f64 variables are converted as the reference converts them. */
+int mr_bathymetry_open(const char *path, const char *x_name, const char *y_name,
+                       const char *depth_name, mr_bathymetry **out);
+
+/* ConstantDepth (src/bathymetry/constant_depth.rs:98-129). */
+int mr_bathymetry_constant(float h, mr_bathymetry **out);
+
+/* ConstantSlope (src/bathymetry/constant_slope.rs:28-77). */
+int mr_bathymetry_slope(float h0, float x0, float y0, float dhdx, float dhdy,
+                        mr_bathymetry **out);
+
+/* ArrayDepth test field (src/bathymetry/array_depth.rs:9-35): n x n values,
+ * arr[i*n + j] = array[i][j]. */
+int mr_bathymetry_array(size_t n, const float *arr, mr_bathymetry **out);
+
+void mr_bathymetry_destroy(mr_bathymetry *b);
+
+/* ---- current ------------------------------------------------------------- */
+
+/* Gridded current (replaces CartesianCurrent, src/current/
+ * cartesian_current.rs:18-27 and :58-213): f64 axes and u, v with flat index
+ * nx*j + i (:421-427).  nx, ny >= 2. */
+int mr_current_grid(size_t nx, size_t ny, const double *x, const double *y,
+                    const double *u, size_t u_len, const double *v,
+                    size_t v_len, mr_current **out);
+
+/* CartesianCurrent::open(path, x_name, y_name, u_name, v_name)
+ * (cartesian_current.rs:58-213). */
+int mr_current_open(const char *path, const char *x_name, const char *y_name,
+                    const char *u_name, const char *v_name, mr_current **out);
+
+/* ConstantCurrent (src/current/constant_current.rs:50-108); (0, 0) is the
+ * reference's DEFAULT_CURRENT (:41). */
+int mr_current_constant(double u, double v, mr_current **out);
+
+void mr_current_destroy(mr_current *c);
+
+/* ---- tracing ------------------------------------------------------------- */
+
+/* Number of RK4 steps: ceil((t_end - t0) / dt) cast as Rust casts to usize
+ * (saturating, NaN -> 0).  A trace call needs rows_cap >= this + 1. */
+uint64_t mr_num_steps(double t0, double t_end, double dt);
+
+/* ManyRays::new(bathymetry, current, rays).trace_many(t0, t_end, dt)
+ * (src/ray.rs:98-127) on the GPU, plain FP64 form.  Host buffers: x0, y0,
+ * kx0, ky0 [n]; traj [5][rows_cap][n]; n_rows [n]; status [n].  Synchronous.
+ * Page-locked output buffers are written by the kernel directly. */
+int mr_trace(const mr_bathymetry *b, const mr_current *c, size_t n,
+             const double *x0, const double *y0, const double *kx0,
+             const double *ky0, double t0, double t_end, double dt,
+             int stop_rule, size_t rows_cap, double *traj, int32_t *n_rows,
+             uint8_t *status);
+
+/* Same, all buffers in device memory; asynchronous on `stream` (a
+ * cudaStream_t; NULL = the calling thread's default stream).  One kernel
+ * launch, no allocation. */
+int mr_trace_device(const mr_bathymetry *b, const mr_current *c, size_t n,
+                    const double *x0, const double *y0, const double *kx0,
+                    const double *ky0, double t0, double t_end, double dt,
+                    int stop_rule, size_t rows_cap, double *traj,
+                    int32_t *n_rows, uint8_t *status, void *stream);
+
+/* SingleRay::trace_individual(0, duration, step_size) as returned by the
+ * extension's single_ray (src/ffi.rs:25-49): rows[rows_cap][5] of
+ * (t, x, y, kx, ky) tuples, *n_rows of them valid. */
+int mr_single_ray(const mr_bathymetry *b, const mr_current *c, double x0,
+                  double y0, double kx0, double ky0, double duration,
+                  double step_size, size_t rows_cap, double *rows,
+                  int32_t *n_rows);
+
+/* _mantaray.single_ray(x0, y0, kx0, ky0, duration, step_size, bathymetry,
+ * current) (src/ffi.rs:25-49): opens the two NetCDF-3 files with the
+ * reference's fixed variable names (x, y, depth; x, y, u, v). */
+int mr_single_ray_files(const char *bathymetry_path, const char *current_path,
+                        double x0, double y0, double kx0, double ky0,
+                        double duration, double step_size, size_t rows_cap,
+                        double *rows, int32_t *n_rows);
+
+/* _mantaray.ray_tracing(x0, y0, kx0, ky0, duration, step_size, bathymetry,
+ * current) (src/ffi.rs:51-85), traj layout as mr_trace. */
+int mr_ray_tracing_files(const char *bathymetry_path, const char *current_path,
+                         size_t n, const double *x0, const double *y0,
+                         const double *kx0, const double *ky0,
+                         double duration, double step_size, size_t rows_cap,
+                         double *traj, int32_t *n_rows, uint8_t *status);
+
+/* ---- NetCDF-3 access (host only, no GPU) ---------------------------------- */
+
+/* Reads variable `name` of a NetCDF-3 file converted to f64 (the reference's
+ * `as f64` conversions).  Writes min(len, cap) values; *len = its length;
+ * *nc_type = its NetCDF type code (1 byte, 2 char/u8, 3 short, 4 int,
+ * 5 float, 6 double). */
+int mr_netcdf3_read_f64(const char *path, const char *name, double *out,
+                        size_t cap, size_t *len, int *nc_type);
+
+/* ---- diagnostics ----------------------------------------------------------- */
+
+/* Message of the last failing call on this thread ("" if none). */
+const char *mr_last_error(void);
+
+/* Measured FMA throughput of the current device in TFLOP/s (fp64 != 0: the
+ * FP64 pipe, else FP32), from a chain-of-FMA kernel on every SM.  The
+ * roofline denominator for the compute-bound integrators.  No counterpart in
+ * the reference (measurement only). */
+int mr_measure_fma_peak(int fp64, double *tflops);
+
+/* Library version, major*10000 + minor*100 + patch. */
+int mr_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MANTARAY_GPU_H */

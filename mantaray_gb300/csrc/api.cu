@@ -1,0 +1,517 @@
+// api.cu -- the C ABI of libmantaray_gpu.so (include/mantaray_gpu.h).
+//
+// Host side of the drop-in: field handles staged once into HBM, argument
+// checking, the reference's step count, launches of the plain FP64 kernel,
+// and the file-path entry points of src/ffi.rs.
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/mantaray_gpu.h"
+#include "fields.h"
+#include "kernels.h"
+#include "netcdf3.h"
+
+struct mr_bathymetry {
+  mr::BathyDev dev{};
+  int device = 0;
+  bool one_point_axis = false;  // the reference panics on its first lookup
+  void *mem[4] = {nullptr, nullptr, nullptr, nullptr};
+};
+
+struct mr_current {
+  mr::CurrentDev dev{};
+  int device = 0;
+  bool one_point_axis = false;
+  void *mem[4] = {nullptr, nullptr, nullptr, nullptr};
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char *fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+  return fail(e == cudaErrorMemoryAllocation ? MR_ERR_OUT_OF_MEMORY : MR_ERR_CUDA, "%s: %s (%s)",
+              what, cudaGetErrorString(e), cudaGetErrorName(e));
+}
+
+#define MR_CUDA(call)                                   \
+  do {                                                  \
+    cudaError_t e_ = (call);                            \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+  } while (0)
+
+// Makes `device` current for the lifetime of the guard.
+class DeviceGuard {
+ public:
+  explicit DeviceGuard(int device) {
+    ok_ = cudaGetDevice(&prev_) == cudaSuccess;
+    if (ok_ && prev_ != device) ok_ = cudaSetDevice(device) == cudaSuccess;
+    switched_ = ok_ && prev_ != device;
+  }
+  ~DeviceGuard() {
+    if (switched_) cudaSetDevice(prev_);
+  }
+  bool ok() const { return ok_; }
+
+ private:
+  int prev_ = 0;
+  bool ok_ = false;
+  bool switched_ = false;
+};
+
+// Device copies of host arrays, freed by the handle destructor.
+template <typename T>
+cudaError_t upload(const T *src, size_t count, void **slot) {
+  if (count == 0) return cudaSuccess;
+  cudaError_t e = cudaMalloc(slot, count * sizeof(T));
+  if (e != cudaSuccess) return e;
+  return cudaMemcpy(*slot, src, count * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+void free_mem(void *const *mem, int count) {
+  for (int i = 0; i < count; ++i)
+    if (mem[i]) cudaFree(mem[i]);
+}
+
+// Keep freed stream-ordered allocations pooled across calls (set once per
+// device); mr_trace's staging buffers are then reused instead of remapped.
+void keep_pool(int device) {
+  static std::mutex mu;
+  static std::vector<int> done;
+  std::lock_guard<std::mutex> lock(mu);
+  for (int d : done)
+    if (d == device) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    uint64_t threshold = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold);
+  }
+  done.push_back(device);
+}
+
+uint64_t rust_ceil_as_usize(double v) {
+  const double c = ceil(v);
+  if (!(c > 0.0)) return 0;
+  if (c >= 18446744073709551616.0) return UINT64_MAX;
+  return static_cast<uint64_t>(c);
+}
+
+int check_trace_args(const mr_bathymetry *b, const mr_current *c, size_t n, const void *x0,
+                     const void *y0, const void *kx0, const void *ky0, double t0, double t_end,
+                     double dt, int stop_rule, size_t rows_cap, const void *traj,
+                     const void *n_rows, const void *status, uint64_t *nsteps) {
+  if (!b || !c) return fail(MR_ERR_INVALID_ARGUMENT, "null field handle");
+  if (b->one_point_axis || c->one_point_axis)
+    return fail(MR_ERR_INVALID_ARGUMENT,
+                "a grid axis has a single point (the reference panics on its first lookup)");
+  if (b->device != c->device)
+    return fail(MR_ERR_INVALID_ARGUMENT, "bathymetry and current live on different devices");
+  if (stop_rule != MR_STOP_STAGE1 && stop_rule != MR_STOP_FRESH)
+    return fail(MR_ERR_INVALID_ARGUMENT, "unknown stop rule %d", stop_rule);
+  if (n > 0 && (!x0 || !y0 || !kx0 || !ky0 || !traj || !n_rows || !status))
+    return fail(MR_ERR_INVALID_ARGUMENT, "null array argument");
+  *nsteps = mr_num_steps(t0, t_end, dt);
+  if (*nsteps >= static_cast<uint64_t>(INT32_MAX))
+    return fail(MR_ERR_CAPACITY, "%llu steps exceed the row counter range",
+                static_cast<unsigned long long>(*nsteps));
+  if (rows_cap < *nsteps + 1)
+    return fail(MR_ERR_CAPACITY, "rows_cap %zu < %llu steps + 1", rows_cap,
+                static_cast<unsigned long long>(*nsteps));
+  return MR_OK;
+}
+
+// Device-visible alias of a host buffer when it is page-locked, else null.
+void *mapped_host(void *p) {
+  cudaPointerAttributes attr;
+  if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (attr.type == cudaMemoryTypeHost && attr.devicePointer) return attr.devicePointer;
+  return nullptr;
+}
+
+void fill_bathy_grid_scalars(mr_bathymetry *h, const float *x, const float *y, size_t nx,
+                             size_t ny) {
+  mr::BathyDev &d = h->dev;
+  d.nx = nx;
+  d.ny = ny;
+  h->one_point_axis = nx < 2 || ny < 2;
+  if (h->one_point_axis) return;
+  // nearest(), cartesian_netcdf3.rs:287-291 (f32)
+  d.x0 = x[0];
+  d.xsp = fabsf(x[1] - x[0]);
+  d.xhigh = static_cast<float>(nx - 1);
+  d.y0 = y[0];
+  d.ysp = fabsf(y[1] - y[0]);
+  d.yhigh = static_cast<float>(ny - 1);
+  // gradient spacing, cartesian_netcdf3.rs:119-120 (f64)
+  d.xspace = static_cast<double>(x[1]) - static_cast<double>(x[0]);
+  d.yspace = static_cast<double>(y[1]) - static_cast<double>(y[0]);
+}
+
+int make_bathy_grid(size_t nx, size_t ny, const float *x, const float *y, const double *depth,
+                    size_t depth_len, mr_bathymetry **out) {
+  if (!out) return fail(MR_ERR_INVALID_ARGUMENT, "null output handle pointer");
+  *out = nullptr;
+  if (nx == 0 || ny == 0 || !x || !y || (depth_len && !depth))
+    return fail(MR_ERR_INVALID_ARGUMENT, "empty axis or null array");
+  int device = 0;
+  MR_CUDA(cudaGetDevice(&device));
+  mr_bathymetry *h = new mr_bathymetry();
+  h->dev.kind = mr::BATHY_GRID;
+  h->device = device;
+  cudaError_t e;
+  if ((e = upload(x, nx, &h->mem[0])) != cudaSuccess ||
+      (e = upload(y, ny, &h->mem[1])) != cudaSuccess ||
+      (e = upload(depth, depth_len, &h->mem[2])) != cudaSuccess) {
+    free_mem(h->mem, 4);
+    delete h;
+    return cuda_fail(e, "staging bathymetry grid");
+  }
+  h->dev.x = static_cast<const float *>(h->mem[0]);
+  h->dev.y = static_cast<const float *>(h->mem[1]);
+  h->dev.depth = static_cast<const double *>(h->mem[2]);
+  h->dev.depth_len = depth_len;
+  fill_bathy_grid_scalars(h, x, y, nx, ny);
+  *out = h;
+  return MR_OK;
+}
+
+int make_current_grid(size_t nx, size_t ny, const double *x, const double *y, const double *u,
+                      size_t u_len, const double *v, size_t v_len, mr_current **out) {
+  if (!out) return fail(MR_ERR_INVALID_ARGUMENT, "null output handle pointer");
+  *out = nullptr;
+  if (nx == 0 || ny == 0 || !x || !y || (u_len && !u) || (v_len && !v))
+    return fail(MR_ERR_INVALID_ARGUMENT, "empty axis or null array");
+  int device = 0;
+  MR_CUDA(cudaGetDevice(&device));
+  mr_current *h = new mr_current();
+  h->dev.kind = mr::CURRENT_GRID;
+  h->device = device;
+  cudaError_t e;
+  if ((e = upload(x, nx, &h->mem[0])) != cudaSuccess ||
+      (e = upload(y, ny, &h->mem[1])) != cudaSuccess ||
+      (e = upload(u, u_len, &h->mem[2])) != cudaSuccess ||
+      (e = upload(v, v_len, &h->mem[3])) != cudaSuccess) {
+    free_mem(h->mem, 4);
+    delete h;
+    return cuda_fail(e, "staging current grid");
+  }
+  mr::CurrentDev &d = h->dev;
+  d.x = static_cast<const double *>(h->mem[0]);
+  d.y = static_cast<const double *>(h->mem[1]);
+  d.u = static_cast<const double *>(h->mem[2]);
+  d.v = static_cast<const double *>(h->mem[3]);
+  d.u_len = u_len;
+  d.v_len = v_len;
+  d.nx = nx;
+  d.ny = ny;
+  h->one_point_axis = nx < 2 || ny < 2;
+  if (!h->one_point_axis) {
+    // nearest(), cartesian_current.rs:244-248 and gradient spacing :515-516
+    d.x0 = x[0];
+    d.xsp = fabs(x[1] - x[0]);
+    d.xhigh = static_cast<double>(nx - 1);
+    d.y0 = y[0];
+    d.ysp = fabs(y[1] - y[0]);
+    d.yhigh = static_cast<double>(ny - 1);
+    d.xspace = x[1] - x[0];
+    d.yspace = y[1] - y[0];
+  }
+  *out = h;
+  return MR_OK;
+}
+
+int launch(const mr_bathymetry *b, const mr_current *c, size_t n, const double *x0,
+           const double *y0, const double *kx0, const double *ky0, double t0, double dt,
+           uint64_t nsteps, int stop_rule, size_t rows_cap, double *traj, int32_t *n_rows,
+           uint8_t *status, cudaStream_t stream) {
+  mr::TraceArgs a;
+  a.n = n;
+  a.x0 = x0; a.y0 = y0; a.kx0 = kx0; a.ky0 = ky0;
+  a.t0 = t0;
+  a.dt = dt;
+  a.nsteps = nsteps;
+  a.rows_cap = rows_cap;
+  a.traj = traj;
+  a.n_rows = n_rows;
+  a.status = status;
+  cudaError_t e = mr::launch_rk4_f64(b->dev, c->dev, a, stop_rule, stream);
+  if (e != cudaSuccess) return cuda_fail(e, "rk4_f64 launch");
+  return MR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *mr_last_error(void) { return g_last_error.c_str(); }
+
+int mr_version(void) { return 100; }
+
+uint64_t mr_num_steps(double t0, double t_end, double dt) {
+  return rust_ceil_as_usize((t_end - t0) / dt);
+}
+
+int mr_bathymetry_grid(size_t nx, size_t ny, const float *x, const float *y, const double *depth,
+                       size_t depth_len, mr_bathymetry **out) {
+  return make_bathy_grid(nx, ny, x, y, depth, depth_len, out);
+}
+
+int mr_bathymetry_open(const char *path, const char *x_name, const char *y_name,
+                       const char *depth_name, mr_bathymetry **out) {
+  if (!path || !x_name || !y_name || !depth_name || !out)
+    return fail(MR_ERR_INVALID_ARGUMENT, "null argument");
+  std::vector<double> xd, yd, depth;
+  std::vector<float> x, y;
+  int type = 0;
+  mr::nc3::Result r = mr::nc3::read_variable(path, x_name, &xd, &type, &x);
+  if (!r.code) r = mr::nc3::read_variable(path, y_name, &yd, &type, &y);
+  if (!r.code) r = mr::nc3::read_variable(path, depth_name, &depth, &type);
+  if (r.code) return fail(r.code, "%s", r.message.c_str());
+  return make_bathy_grid(x.size(), y.size(), x.data(), y.data(), depth.data(), depth.size(), out);
+}
+
+int mr_bathymetry_constant(float h, mr_bathymetry **out) {
+  if (!out) return fail(MR_ERR_INVALID_ARGUMENT, "null output handle pointer");
+  int device = 0;
+  MR_CUDA(cudaGetDevice(&device));
+  mr_bathymetry *b = new mr_bathymetry();
+  b->device = device;
+  b->dev.kind = mr::BATHY_CONSTANT;
+  b->dev.h = h;
+  *out = b;
+  return MR_OK;
+}
+
+int mr_bathymetry_slope(float h0, float x0, float y0, float dhdx, float dhdy,
+                        mr_bathymetry **out) {
+  if (!out) return fail(MR_ERR_INVALID_ARGUMENT, "null output handle pointer");
+  int device = 0;
+  MR_CUDA(cudaGetDevice(&device));
+  mr_bathymetry *b = new mr_bathymetry();
+  b->device = device;
+  b->dev.kind = mr::BATHY_SLOPE;
+  b->dev.s_h0 = h0; b->dev.s_x0 = x0; b->dev.s_y0 = y0;
+  b->dev.s_dhdx = dhdx; b->dev.s_dhdy = dhdy;
+  *out = b;
+  return MR_OK;
+}
+
+int mr_bathymetry_array(size_t n, const float *arr, mr_bathymetry **out) {
+  if (!out) return fail(MR_ERR_INVALID_ARGUMENT, "null output handle pointer");
+  *out = nullptr;
+  if (n && !arr) return fail(MR_ERR_INVALID_ARGUMENT, "null array");
+  int device = 0;
+  MR_CUDA(cudaGetDevice(&device));
+  mr_bathymetry *b = new mr_bathymetry();
+  b->device = device;
+  b->dev.kind = mr::BATHY_ARRAY;
+  b->dev.an = n;
+  cudaError_t e = upload(arr, n * n, &b->mem[0]);
+  if (e != cudaSuccess) {
+    delete b;
+    return cuda_fail(e, "staging array depth");
+  }
+  b->dev.arr = static_cast<const float *>(b->mem[0]);
+  *out = b;
+  return MR_OK;
+}
+
+void mr_bathymetry_destroy(mr_bathymetry *b) {
+  if (!b) return;
+  DeviceGuard g(b->device);
+  free_mem(b->mem, 4);
+  delete b;
+}
+
+int mr_current_grid(size_t nx, size_t ny, const double *x, const double *y, const double *u,
+                    size_t u_len, const double *v, size_t v_len, mr_current **out) {
+  return make_current_grid(nx, ny, x, y, u, u_len, v, v_len, out);
+}
+
+int mr_current_open(const char *path, const char *x_name, const char *y_name, const char *u_name,
+                    const char *v_name, mr_current **out) {
+  if (!path || !x_name || !y_name || !u_name || !v_name || !out)
+    return fail(MR_ERR_INVALID_ARGUMENT, "null argument");
+  std::vector<double> x, y, u, v;
+  int type = 0;
+  mr::nc3::Result r = mr::nc3::read_variable(path, x_name, &x, &type);
+  if (!r.code) r = mr::nc3::read_variable(path, y_name, &y, &type);
+  if (!r.code) r = mr::nc3::read_variable(path, u_name, &u, &type);
+  if (!r.code) r = mr::nc3::read_variable(path, v_name, &v, &type);
+  if (r.code) return fail(r.code, "%s", r.message.c_str());
+  return make_current_grid(x.size(), y.size(), x.data(), y.data(), u.data(), u.size(), v.data(),
+                           v.size(), out);
+}
+
+int mr_current_constant(double u, double v, mr_current **out) {
+  if (!out) return fail(MR_ERR_INVALID_ARGUMENT, "null output handle pointer");
+  int device = 0;
+  MR_CUDA(cudaGetDevice(&device));
+  mr_current *c = new mr_current();
+  c->device = device;
+  c->dev.kind = mr::CURRENT_CONSTANT;
+  c->dev.cu = u;
+  c->dev.cv = v;
+  *out = c;
+  return MR_OK;
+}
+
+void mr_current_destroy(mr_current *c) {
+  if (!c) return;
+  DeviceGuard g(c->device);
+  free_mem(c->mem, 4);
+  delete c;
+}
+
+int mr_trace_device(const mr_bathymetry *b, const mr_current *c, size_t n, const double *x0,
+                    const double *y0, const double *kx0, const double *ky0, double t0,
+                    double t_end, double dt, int stop_rule, size_t rows_cap, double *traj,
+                    int32_t *n_rows, uint8_t *status, void *stream) {
+  uint64_t nsteps = 0;
+  int rc = check_trace_args(b, c, n, x0, y0, kx0, ky0, t0, t_end, dt, stop_rule, rows_cap, traj,
+                            n_rows, status, &nsteps);
+  if (rc) return rc;
+  if (n == 0) return MR_OK;
+  DeviceGuard g(b->device);
+  if (!g.ok()) return fail(MR_ERR_CUDA, "cannot select device %d", b->device);
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : cudaStreamPerThread;
+  return launch(b, c, n, x0, y0, kx0, ky0, t0, dt, nsteps, stop_rule, rows_cap, traj, n_rows,
+                status, s);
+}
+
+int mr_trace(const mr_bathymetry *b, const mr_current *c, size_t n, const double *x0,
+             const double *y0, const double *kx0, const double *ky0, double t0, double t_end,
+             double dt, int stop_rule, size_t rows_cap, double *traj, int32_t *n_rows,
+             uint8_t *status) {
+  uint64_t nsteps = 0;
+  int rc = check_trace_args(b, c, n, x0, y0, kx0, ky0, t0, t_end, dt, stop_rule, rows_cap, traj,
+                            n_rows, status, &nsteps);
+  if (rc) return rc;
+  if (n == 0) return MR_OK;
+  DeviceGuard g(b->device);
+  if (!g.ok()) return fail(MR_ERR_CUDA, "cannot select device %d", b->device);
+  keep_pool(b->device);
+  cudaStream_t s = cudaStreamPerThread;
+  const size_t traj_bytes = 5 * rows_cap * n * sizeof(double);
+  // Inputs: one staging block for the four initial-state arrays.
+  double *d_in = nullptr;
+  MR_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&d_in), 4 * n * sizeof(double), s));
+  const double *srcs[4] = {x0, y0, kx0, ky0};
+  for (int q = 0; q < 4; ++q) {
+    cudaError_t e = cudaMemcpyAsync(d_in + q * n, srcs[q], n * sizeof(double),
+                                    cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) {
+      cudaFreeAsync(d_in, s);
+      return cuda_fail(e, "copying initial states to the device");
+    }
+  }
+  // Outputs: written in place when the caller's buffers are page-locked,
+  // else through device buffers copied back after the launch.
+  double *d_traj = static_cast<double *>(mapped_host(traj));
+  int32_t *d_rows = static_cast<int32_t *>(mapped_host(n_rows));
+  uint8_t *d_status = static_cast<uint8_t *>(mapped_host(status));
+  const bool own_traj = !d_traj, own_rows = !d_rows, own_status = !d_status;
+  cudaError_t e = cudaSuccess;
+  if (own_traj) e = cudaMallocAsync(reinterpret_cast<void **>(&d_traj), traj_bytes, s);
+  if (e == cudaSuccess && own_rows)
+    e = cudaMallocAsync(reinterpret_cast<void **>(&d_rows), n * sizeof(int32_t), s);
+  if (e == cudaSuccess && own_status) e = cudaMallocAsync(reinterpret_cast<void **>(&d_status), n, s);
+  if (e == cudaSuccess) {
+    rc = launch(b, c, n, d_in, d_in + n, d_in + 2 * n, d_in + 3 * n, t0, dt, nsteps, stop_rule,
+                rows_cap, d_traj, d_rows, d_status, s);
+  } else {
+    rc = cuda_fail(e, "allocating device output buffers");
+  }
+  if (rc == MR_OK && own_traj) e = cudaMemcpyAsync(traj, d_traj, traj_bytes, cudaMemcpyDeviceToHost, s);
+  if (rc == MR_OK && e == cudaSuccess && own_rows)
+    e = cudaMemcpyAsync(n_rows, d_rows, n * sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+  if (rc == MR_OK && e == cudaSuccess && own_status)
+    e = cudaMemcpyAsync(status, d_status, n, cudaMemcpyDeviceToHost, s);
+  if (rc == MR_OK && e != cudaSuccess) rc = cuda_fail(e, "copying trajectories to the host");
+  cudaError_t se = cudaStreamSynchronize(s);
+  if (rc == MR_OK && se != cudaSuccess) rc = cuda_fail(se, "rk4_f64 execution");
+  cudaFreeAsync(d_in, s);
+  if (own_traj && d_traj) cudaFreeAsync(d_traj, s);
+  if (own_rows && d_rows) cudaFreeAsync(d_rows, s);
+  if (own_status && d_status) cudaFreeAsync(d_status, s);
+  return rc;
+}
+
+int mr_single_ray(const mr_bathymetry *b, const mr_current *c, double x0, double y0, double kx0,
+                  double ky0, double duration, double step_size, size_t rows_cap, double *rows,
+                  int32_t *n_rows) {
+  if (!rows || !n_rows) return fail(MR_ERR_INVALID_ARGUMENT, "null output");
+  std::vector<double> traj(5 * rows_cap);
+  uint8_t status = 0;
+  int rc = mr_trace(b, c, 1, &x0, &y0, &kx0, &ky0, 0.0, duration, step_size, MR_STOP_STAGE1,
+                    rows_cap, traj.data(), n_rows, &status);
+  if (rc) return rc;
+  for (size_t r = 0; r < rows_cap; ++r)
+    for (int v = 0; v < 5; ++v) rows[r * 5 + v] = traj[v * rows_cap + r];
+  return MR_OK;
+}
+
+int mr_single_ray_files(const char *bathymetry_path, const char *current_path, double x0,
+                        double y0, double kx0, double ky0, double duration, double step_size,
+                        size_t rows_cap, double *rows, int32_t *n_rows) {
+  mr_bathymetry *b = nullptr;
+  mr_current *c = nullptr;
+  int rc = mr_bathymetry_open(bathymetry_path, "x", "y", "depth", &b);
+  if (!rc) rc = mr_current_open(current_path, "x", "y", "u", "v", &c);
+  if (!rc) rc = mr_single_ray(b, c, x0, y0, kx0, ky0, duration, step_size, rows_cap, rows, n_rows);
+  mr_bathymetry_destroy(b);
+  mr_current_destroy(c);
+  return rc;
+}
+
+int mr_ray_tracing_files(const char *bathymetry_path, const char *current_path, size_t n,
+                         const double *x0, const double *y0, const double *kx0,
+                         const double *ky0, double duration, double step_size, size_t rows_cap,
+                         double *traj, int32_t *n_rows, uint8_t *status) {
+  mr_bathymetry *b = nullptr;
+  mr_current *c = nullptr;
+  int rc = mr_bathymetry_open(bathymetry_path, "x", "y", "depth", &b);
+  if (!rc) rc = mr_current_open(current_path, "x", "y", "u", "v", &c);
+  if (!rc)
+    rc = mr_trace(b, c, n, x0, y0, kx0, ky0, 0.0, duration, step_size, MR_STOP_STAGE1, rows_cap,
+                  traj, n_rows, status);
+  mr_bathymetry_destroy(b);
+  mr_current_destroy(c);
+  return rc;
+}
+
+int mr_netcdf3_read_f64(const char *path, const char *name, double *out, size_t cap, size_t *len,
+                        int *nc_type) {
+  if (!path || !name || !len) return fail(MR_ERR_INVALID_ARGUMENT, "null argument");
+  std::vector<double> v;
+  int type = 0;
+  mr::nc3::Result r = mr::nc3::read_variable(path, name, &v, &type);
+  if (r.code) return fail(r.code, "%s", r.message.c_str());
+  *len = v.size();
+  if (nc_type) *nc_type = type;
+  if (out) memcpy(out, v.data(), (cap < v.size() ? cap : v.size()) * sizeof(double));
+  return MR_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,29 @@
+// kernels.h -- launch interfaces of the device kernels (internal to the
+// library; the public C ABI is include/mantaray_gpu.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fields.h"
+
+namespace mr {
+
+constexpr int kK1Block = 64;
+
+// Arguments of one trace launch.  All pointers are device-visible.
+struct TraceArgs {
+  uint64_t n;                 // rays
+  const double *x0, *y0, *kx0, *ky0;
+  double t0, dt;
+  uint64_t nsteps;            // ceil((t_end - t0) / dt) as usize
+  uint64_t rows_cap;          // rows per ray in traj (>= nsteps + 1)
+  double *traj;               // [5][rows_cap][n]: t, x, y, kx, ky
+  int32_t *n_rows;            // [n]
+  uint8_t *status;            // [n]
+};
+
+cudaError_t launch_rk4_f64(const BathyDev &b, const CurrentDev &c, const TraceArgs &a,
+                           int stop_rule, cudaStream_t stream);
+
+}  // namespace mr

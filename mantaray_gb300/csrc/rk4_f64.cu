@@ -1,0 +1,117 @@
+// rk4_f64.cu -- K1, the plain FP64 ray integrator (the drop-in form).
+//
+// One ray per thread.  Each thread runs the reference stepper
+// (ode_solvers 0.4.0 Rk4, called from src/ray.rs:198-213) on the reference
+// right-hand side (ray_exact.cuh).  Trajectories are written time-major per
+// variable, traj[v][row][ray] (v = t, x, y, kx, ky), which is the
+// (time_step, ray) layout of the reference's xarray result
+// (python/mantaray/core.py:114-125): at every step a warp stores 32
+// consecutive doubles per variable (fully coalesced 256-byte rows).  Rows after
+// a ray's last row are NaN, as the Python wrapper pads them.
+//
+// Compiled with -fmad=false: no contraction anywhere in this file.
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "kernels.h"
+#include "ray_exact.cuh"
+
+namespace mr {
+
+namespace {
+
+__device__ __forceinline__ void store_row(double *traj, uint64_t plane, uint64_t n,
+                                          uint64_t row, uint64_t i, double t,
+                                          const double y[4]) {
+  double *p = traj + row * n + i;
+  p[0] = t;
+  p[plane] = y[0];
+  p[2 * plane] = y[1];
+  p[3 * plane] = y[2];
+  p[4 * plane] = y[3];
+}
+
+__device__ __forceinline__ void store_nan_row(double *traj, uint64_t plane, uint64_t n,
+                                              uint64_t row, uint64_t i) {
+  const double nan = __longlong_as_double(0x7ff8000000000000ll);
+  double *p = traj + row * n + i;
+#pragma unroll
+  for (int v = 0; v < 5; ++v) p[v * plane] = nan;
+}
+
+template <int STOP_RULE>
+__global__ void __launch_bounds__(kK1Block) rk4_f64_kernel(BathyDev b, CurrentDev c,
+                                                           TraceArgs a) {
+  const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  const bool valid = i < a.n;
+  const uint64_t plane = a.rows_cap * a.n;
+  double y[4] = {0.0, 0.0, 0.0, 0.0};
+  double k1[4] = {0.0, 0.0, 0.0, 0.0};
+  double t = a.t0;
+  bool alive = valid;
+  uint64_t rows = 0;
+  if (valid) {
+    y[0] = a.x0[i]; y[1] = a.y0[i]; y[2] = a.kx0[i]; y[3] = a.ky0[i];
+    store_row(a.traj, plane, a.n, 0, i, t, y);
+    rows = 1;
+    system_exact(b, c, y, k1);
+  }
+  const double half = a.dt / 2.0;
+  const double sixth = a.dt / 6.0;
+  uint64_t s = 0;
+  for (; s < a.nsteps; ++s) {
+    // Once every lane of the warp has stopped, the rest is NaN padding.
+    if (__all_sync(0xffffffffu, !alive)) break;
+    if (alive) {
+      double k2[4], k3[4], k4[4], tmp[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) tmp[q] = y[q] + k1[q] * half;
+      system_exact(b, c, tmp, k2);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) tmp[q] = y[q] + k2[q] * half;
+      system_exact(b, c, tmp, k3);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) tmp[q] = y[q] + k3[q] * a.dt;
+      system_exact(b, c, tmp, k4);
+      double yn[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) yn[q] = y[q] + (k1[q] + k2[q] * 2.0 + k3[q] * 2.0 + k4[q]) * sixth;
+      t = t + a.dt;
+      store_row(a.traj, plane, a.n, s + 1, i, t, yn);
+      ++rows;
+      // The next step's first stage doubles as the FRESH stop-rule derivative
+      // (system() does not depend on t).
+      double fresh[4];
+      system_exact(b, c, yn, fresh);
+      const bool stop = STOP_RULE == 1 ? (all_nan4(fresh) || all_nan4(yn))
+                                       : (all_nan4(k1) || all_nan4(yn));
+#pragma unroll
+      for (int q = 0; q < 4; ++q) { y[q] = yn[q]; k1[q] = fresh[q]; }
+      if (stop) alive = false;
+    } else if (valid) {
+      store_nan_row(a.traj, plane, a.n, s + 1, i);
+    }
+  }
+  if (valid) {
+    for (uint64_t row = rows > s + 1 ? rows : s + 1; row < a.rows_cap; ++row)
+      store_nan_row(a.traj, plane, a.n, row, i);
+    a.n_rows[i] = static_cast<int32_t>(rows);
+    a.status[i] = alive ? 0 : 1;
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_rk4_f64(const BathyDev &b, const CurrentDev &c, const TraceArgs &a,
+                           int stop_rule, cudaStream_t stream) {
+  if (a.n == 0) return cudaSuccess;
+  const unsigned grid = static_cast<unsigned>((a.n + kK1Block - 1) / kK1Block);
+  if (stop_rule == 1)
+    rk4_f64_kernel<1><<<grid, kK1Block, 0, stream>>>(b, c, a);
+  else
+    rk4_f64_kernel<0><<<grid, kK1Block, 0, stream>>>(b, c, a);
+  return cudaGetLastError();
+}
+
+}  // namespace mr
