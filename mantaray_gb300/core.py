@@ -22,8 +22,17 @@ from .fields import Bathymetry, Current
 
 VARNAMES = ("time", "x", "y", "kx", "ky")
 
-_STOP_RULES = {"stage1": N.STOP_STAGE1, "fresh": N.STOP_FRESH,
-               N.STOP_STAGE1: N.STOP_STAGE1, N.STOP_FRESH: N.STOP_FRESH}
+_STOP_RULES = {"stage1": N.STOP_STAGE1, "fresh": N.STOP_FRESH}
+
+
+def _stop_rule(rule) -> int:
+    """Named rules map to their codes; integers go to the library as they are
+    (it rejects unknown codes)."""
+    if isinstance(rule, str):
+        if rule not in _STOP_RULES:
+            raise ValueError(f"unknown stop rule {rule!r} (use 'stage1' or 'fresh')")
+        return _STOP_RULES[rule]
+    return int(rule)
 
 
 def num_steps(t0: float, t_end: float, dt: float) -> int:
@@ -75,7 +84,7 @@ def trace(bathymetry: Bathymetry, current: Current, x0, y0, kx0, ky0, duration: 
     status = np.zeros(n, np.uint8)
     N.check(L.mr_trace(bathymetry.handle, current.handle, n, x0.ctypes.data, y0.ctypes.data,
                        kx0.ctypes.data, ky0.ctypes.data, float(t0), float(t_end),
-                       float(step_size), _STOP_RULES[stop_rule], rows_cap, out.ctypes.data,
+                       float(step_size), _stop_rule(stop_rule), rows_cap, out.ctypes.data,
                        n_rows.ctypes.data, status.ctypes.data))
     return TraceResult(out, n_rows, status)
 
@@ -97,7 +106,7 @@ def trace_device(bathymetry: Bathymetry, current: Current, x0, y0, kx0, ky0, t0:
     handle = getattr(stream, "cuda_stream", stream)
     N.check(L.mr_trace_device(bathymetry.handle, current.handle, n, x0.data_ptr(), y0.data_ptr(),
                               kx0.data_ptr(), ky0.data_ptr(), float(t0), float(t_end),
-                              float(step_size), _STOP_RULES[stop_rule], rows_cap,
+                              float(step_size), _stop_rule(stop_rule), rows_cap,
                               traj.data_ptr(), n_rows.data_ptr(), status.data_ptr(),
                               handle))
 
