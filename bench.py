@@ -57,6 +57,8 @@ def parse():
                    help="wall-time budget of the CPU-baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--math", default="identity", choices=["identity", "libm"],
+                   help="right-hand-side arithmetic of the plain FP64 kernel")
     return p.parse_args()
 
 
@@ -216,8 +218,9 @@ def gb300_arm(args, rank: int, world: int, local_rank: int):
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream(dev)
 
-    def one():
-        mr.trace_device(b, c, *ins, w.t0, w.t_end, w.dt, traj, n_rows, status, stream=stream)
+    def one(math=args.math):
+        mr.trace_device(b, c, *ins, w.t0, w.t_end, w.dt, traj, n_rows, status, math=math,
+                        stream=stream)
 
     for _ in range(args.warmup):
         one()
@@ -253,6 +256,22 @@ def gb300_arm(args, rank: int, world: int, local_rank: int):
     value = total_ray_steps / t_max
     kernel_s = local_t / args.steps
 
+    # ---- the other right-hand-side arithmetic, same workload (reported only) ----
+    alt_math = "libm" if args.math == "identity" else "identity"
+    one(alt_math)
+    torch.cuda.synchronize()
+    alt_times = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        one(alt_math)
+        e1.record(stream)
+        e1.synchronize()
+        alt_times.append(e0.elapsed_time(e1) / 1e3)
+    alt_rate = int(torch.sum(n_rows.to(torch.int64) - 1).item()) * args.steps / sum(alt_times)
+
     # ---- end-to-end through the C ABI with host buffers (e2e) ----
     e2e = None
     if not args.no_e2e:
@@ -260,14 +279,14 @@ def gb300_arm(args, rank: int, world: int, local_rank: int):
         hout = torch.empty((5, rows, n), dtype=torch.float64, pin_memory=True)
         hout_np = hout.numpy()
         h_np = [t.numpy() for t in hin]
-        mr.trace(b, c, *h_np, w.t_end - w.t0, w.dt, t0=w.t0, out=hout_np)  # warm-up
+        mr.trace(b, c, *h_np, w.t_end - w.t0, w.dt, t0=w.t0, out=hout_np, math=args.math)  # warm-up
         barrier()
         e2e_times = []
         for _ in range(args.steps):
             flush.fill_(1.0)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            res = mr.trace(b, c, *h_np, w.t_end - w.t0, w.dt, t0=w.t0, out=hout_np)
+            res = mr.trace(b, c, *h_np, w.t_end - w.t0, w.dt, t0=w.t0, out=hout_np, math=args.math)
             e2e_times.append(time.perf_counter() - t0)
         barrier()
         e2e_local = sum(e2e_times)
@@ -333,7 +352,8 @@ def gb300_arm(args, rank: int, world: int, local_rank: int):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": w.name, "form": "plain FP64 (rk4_f64), one launch per call",
                    "rays_per_gpu": n, "steps_per_ray": rows - 1, "grid": "2001x2001 f64 depth/u/v",
-                   "dt": w.dt, "stop_rule": "stage1",
+                   "dt": w.dt, "stop_rule": "stage1", "math": args.math,
+                   "other_math": {"math": alt_math, "value": alt_rate, "unit": METRIC},
                    "l2": "512 MB buffer written between timed steps; each step also writes 10.5 GB",
                    "parallelism": f"replicas x{world}"},
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,

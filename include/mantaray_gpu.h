@@ -57,15 +57,25 @@ extern "C" {
 #define MR_RAY_COMPLETE 0 /* all ceil((t_end - t0)/dt) steps taken */
 #define MR_RAY_STOPPED 1  /* ended by the solout rule (src/wave_ray_path.rs:236-246) */
 
-/* ---- stop rule ----------------------------------------------------------
- * Which derivative the solout test sees after each step.  The stepper crate
- * (ode_solvers 0.4.0) is not in the reference tree, so both readings are
- * offered; they differ only by whether a ray whose new state is finite but
- * out of the domain records one more, all-NaN, row.
+/* ---- trace options (bit flags, OR-ed into `options`) ---------------------
+ * Stop rule: which derivative the solout test sees after each step.  The
+ * stepper crate (ode_solvers 0.4.0) is not in the reference tree, so both
+ * readings are offered; they differ only by whether a ray whose new state is
+ * finite but out of the domain records one more, all-NaN, row.
  *   MR_STOP_STAGE1: the first-stage derivative of the step just taken.
- *   MR_STOP_FRESH:  the derivative evaluated at the new state. */
-#define MR_STOP_STAGE1 0
-#define MR_STOP_FRESH 1
+ *   MR_STOP_FRESH:  the derivative evaluated at the new state.
+ * Right-hand-side arithmetic of the plain FP64 kernel:
+ *   MR_MATH_LIBM:     the reference's own calls (atan2, cos, sin, cosh, tanh,
+ *                     sinh, three sqrt) in its own order.
+ *   MR_MATH_IDENTITY: the same quantities from one expm1, one rsqrt and
+ *                     kx/k, ky/k (exact identities; a few ulps apart), about
+ *                     twice as fast on the FP64 pipe.
+ * Field lookups and interpolation are bit-identical to the reference in
+ * both. */
+#define MR_STOP_STAGE1 0x0
+#define MR_STOP_FRESH 0x1
+#define MR_MATH_LIBM 0x0
+#define MR_MATH_IDENTITY 0x10
 
 typedef struct mr_bathymetry mr_bathymetry;
 typedef struct mr_current mr_current;
@@ -134,7 +144,7 @@ uint64_t mr_num_steps(double t0, double t_end, double dt);
 int mr_trace(const mr_bathymetry *b, const mr_current *c, size_t n,
              const double *x0, const double *y0, const double *kx0,
              const double *ky0, double t0, double t_end, double dt,
-             int stop_rule, size_t rows_cap, double *traj, int32_t *n_rows,
+             int options, size_t rows_cap, double *traj, int32_t *n_rows,
              uint8_t *status);
 
 /* Same, all buffers in device memory; asynchronous on `stream` (a
@@ -143,7 +153,7 @@ int mr_trace(const mr_bathymetry *b, const mr_current *c, size_t n,
 int mr_trace_device(const mr_bathymetry *b, const mr_current *c, size_t n,
                     const double *x0, const double *y0, const double *kx0,
                     const double *ky0, double t0, double t_end, double dt,
-                    int stop_rule, size_t rows_cap, double *traj,
+                    int options, size_t rows_cap, double *traj,
                     int32_t *n_rows, uint8_t *status, void *stream);
 
 /* SingleRay::trace_individual(0, duration, step_size) as returned by the

@@ -22,8 +22,10 @@ ERR_OUT_OF_MEMORY = -6
 RAY_COMPLETE = 0
 RAY_STOPPED = 1
 
-STOP_STAGE1 = 0
-STOP_FRESH = 1
+STOP_STAGE1 = 0x0
+STOP_FRESH = 0x1
+MATH_LIBM = 0x0
+MATH_IDENTITY = 0x10
 
 # Exported symbols (checked by the CPU test that loads the library).
 SYMBOLS = (

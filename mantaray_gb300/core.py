@@ -23,16 +23,21 @@ from .fields import Bathymetry, Current
 VARNAMES = ("time", "x", "y", "kx", "ky")
 
 _STOP_RULES = {"stage1": N.STOP_STAGE1, "fresh": N.STOP_FRESH}
+_MATH = {"libm": N.MATH_LIBM, "identity": N.MATH_IDENTITY}
 
 
-def _stop_rule(rule) -> int:
-    """Named rules map to their codes; integers go to the library as they are
-    (it rejects unknown codes)."""
-    if isinstance(rule, str):
-        if rule not in _STOP_RULES:
-            raise ValueError(f"unknown stop rule {rule!r} (use 'stage1' or 'fresh')")
-        return _STOP_RULES[rule]
-    return int(rule)
+def _options(stop_rule, math) -> int:
+    """Option bits of a trace call.  Named choices map to their bits; integers
+    go to the library as they are (it rejects unknown bits)."""
+    bits = 0
+    for value, table, what in ((stop_rule, _STOP_RULES, "stop rule"), (math, _MATH, "math")):
+        if isinstance(value, str):
+            if value not in table:
+                raise ValueError(f"unknown {what} {value!r} (one of {sorted(table)})")
+            bits |= table[value]
+        else:
+            bits |= int(value)
+    return bits
 
 
 def num_steps(t0: float, t_end: float, dt: float) -> int:
@@ -63,11 +68,13 @@ def _f64(a):
 
 
 def trace(bathymetry: Bathymetry, current: Current, x0, y0, kx0, ky0, duration: float,
-          step_size: float, t0: float = 0.0, stop_rule="stage1", out: np.ndarray | None = None,
-          rows_cap: int | None = None) -> TraceResult:
+          step_size: float, t0: float = 0.0, stop_rule="stage1", math="libm",
+          out: np.ndarray | None = None, rows_cap: int | None = None) -> TraceResult:
     """Traces rays from t0 to t0 + duration with step `step_size` (plain FP64
-    kernel).  `out` may be a preallocated (page-locked for speed) float64
-    array of shape (5, rows_cap, n)."""
+    kernel).  stop_rule: "stage1" or "fresh"; math: "libm" (the reference's
+    transcendental calls) or "identity" (same quantities, fewer FP64
+    instructions).  `out` may be a preallocated (page-locked for speed)
+    float64 array of shape (5, rows_cap, n)."""
     L = N.load()
     x0, y0, kx0, ky0 = (_f64(a) for a in (x0, y0, kx0, ky0))
     n = x0.size
@@ -84,14 +91,14 @@ def trace(bathymetry: Bathymetry, current: Current, x0, y0, kx0, ky0, duration: 
     status = np.zeros(n, np.uint8)
     N.check(L.mr_trace(bathymetry.handle, current.handle, n, x0.ctypes.data, y0.ctypes.data,
                        kx0.ctypes.data, ky0.ctypes.data, float(t0), float(t_end),
-                       float(step_size), _stop_rule(stop_rule), rows_cap, out.ctypes.data,
+                       float(step_size), _options(stop_rule, math), rows_cap, out.ctypes.data,
                        n_rows.ctypes.data, status.ctypes.data))
     return TraceResult(out, n_rows, status)
 
 
 def trace_device(bathymetry: Bathymetry, current: Current, x0, y0, kx0, ky0, t0: float,
                  t_end: float, step_size: float, traj, n_rows, status, stop_rule="stage1",
-                 stream=None) -> None:
+                 math="libm", stream=None) -> None:
     """Device-buffer form: every array argument is a CUDA tensor (torch) or any
     object with `data_ptr()`; traj has shape (5, rows_cap, n).  Asynchronous on
     `stream` (a torch.cuda.Stream, a raw handle, or None for the current
@@ -106,7 +113,7 @@ def trace_device(bathymetry: Bathymetry, current: Current, x0, y0, kx0, ky0, t0:
     handle = getattr(stream, "cuda_stream", stream)
     N.check(L.mr_trace_device(bathymetry.handle, current.handle, n, x0.data_ptr(), y0.data_ptr(),
                               kx0.data_ptr(), ky0.data_ptr(), float(t0), float(t_end),
-                              float(step_size), _stop_rule(stop_rule), rows_cap,
+                              float(step_size), _options(stop_rule, math), rows_cap,
                               traj.data_ptr(), n_rows.data_ptr(), status.data_ptr(),
                               handle))
 

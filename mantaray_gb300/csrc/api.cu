@@ -23,14 +23,14 @@ struct mr_bathymetry {
   mr::BathyDev dev{};
   int device = 0;
   bool one_point_axis = false;  // the reference panics on its first lookup
-  void *mem[4] = {nullptr, nullptr, nullptr, nullptr};
+  std::vector<void *> mem;      // device allocations owned by the handle
 };
 
 struct mr_current {
   mr::CurrentDev dev{};
   int device = 0;
   bool one_point_axis = false;
-  void *mem[4] = {nullptr, nullptr, nullptr, nullptr};
+  std::vector<void *> mem;
 };
 
 namespace {
@@ -77,19 +77,27 @@ class DeviceGuard {
   bool switched_ = false;
 };
 
-// Device copies of host arrays, freed by the handle destructor.
+// Device copy of a host array, owned (and freed) by the handle.
 template <typename T>
-cudaError_t upload(const T *src, size_t count, void **slot) {
+cudaError_t upload(const T *src, size_t count, std::vector<void *> *owner, const T **dst) {
+  *dst = nullptr;
   if (count == 0) return cudaSuccess;
-  cudaError_t e = cudaMalloc(slot, count * sizeof(T));
+  void *p = nullptr;
+  cudaError_t e = cudaMalloc(&p, count * sizeof(T));
   if (e != cudaSuccess) return e;
-  return cudaMemcpy(*slot, src, count * sizeof(T), cudaMemcpyHostToDevice);
+  owner->push_back(p);
+  *dst = static_cast<const T *>(p);
+  return cudaMemcpy(p, src, count * sizeof(T), cudaMemcpyHostToDevice);
 }
 
-void free_mem(void *const *mem, int count) {
-  for (int i = 0; i < count; ++i)
-    if (mem[i]) cudaFree(mem[i]);
+void free_mem(std::vector<void *> &mem) {
+  for (void *p : mem) cudaFree(p);
+  mem.clear();
 }
+
+constexpr int kOptionsMask = MR_STOP_FRESH | MR_MATH_IDENTITY;
+// Options of the reference-shaped entry points (mr_single_ray, the file forms).
+constexpr int kDropInOptions = MR_STOP_STAGE1 | MR_MATH_LIBM;
 
 // Keep freed stream-ordered allocations pooled across calls (set once per
 // device); mr_trace's staging buffers are then reused instead of remapped.
@@ -116,7 +124,7 @@ uint64_t rust_ceil_as_usize(double v) {
 
 int check_trace_args(const mr_bathymetry *b, const mr_current *c, size_t n, const void *x0,
                      const void *y0, const void *kx0, const void *ky0, double t0, double t_end,
-                     double dt, int stop_rule, size_t rows_cap, const void *traj,
+                     double dt, int options, size_t rows_cap, const void *traj,
                      const void *n_rows, const void *status, uint64_t *nsteps) {
   if (!b || !c) return fail(MR_ERR_INVALID_ARGUMENT, "null field handle");
   if (b->one_point_axis || c->one_point_axis)
@@ -124,8 +132,8 @@ int check_trace_args(const mr_bathymetry *b, const mr_current *c, size_t n, cons
                 "a grid axis has a single point (the reference panics on its first lookup)");
   if (b->device != c->device)
     return fail(MR_ERR_INVALID_ARGUMENT, "bathymetry and current live on different devices");
-  if (stop_rule != MR_STOP_STAGE1 && stop_rule != MR_STOP_FRESH)
-    return fail(MR_ERR_INVALID_ARGUMENT, "unknown stop rule %d", stop_rule);
+  if (options & ~kOptionsMask)
+    return fail(MR_ERR_INVALID_ARGUMENT, "unknown option bits 0x%x", options & ~kOptionsMask);
   if (n > 0 && (!x0 || !y0 || !kx0 || !ky0 || !traj || !n_rows || !status))
     return fail(MR_ERR_INVALID_ARGUMENT, "null array argument");
   *nsteps = mr_num_steps(t0, t_end, dt);
@@ -179,19 +187,33 @@ int make_bathy_grid(size_t nx, size_t ny, const float *x, const float *y, const 
   mr_bathymetry *h = new mr_bathymetry();
   h->dev.kind = mr::BATHY_GRID;
   h->device = device;
+  fill_bathy_grid_scalars(h, x, y, nx, ny);
+  // Tables (fields.h): depth as f32, and the f32 cell gradients of
+  // cartesian_netcdf3.rs:119-134 for every cell whose corners are in range.
+  std::vector<float> d32(depth_len), gx(depth_len, 0.0f), gy(depth_len, 0.0f);
+  for (size_t i = 0; i < depth_len; ++i) d32[i] = static_cast<float>(depth[i]);
+  if (!h->one_point_axis) {
+    for (size_t j = 0; j + 1 < ny; ++j) {
+      for (size_t i = 0; i + 1 < nx; ++i) {
+        const size_t sw = nx * j + i;
+        if (nx * (j + 1) + i + 1 >= depth_len) continue;
+        gx[sw] = static_cast<float>((depth[sw + 1] - depth[sw]) / h->dev.xspace);
+        gy[sw] = static_cast<float>((depth[sw + nx] - depth[sw]) / h->dev.yspace);
+      }
+    }
+  }
   cudaError_t e;
-  if ((e = upload(x, nx, &h->mem[0])) != cudaSuccess ||
-      (e = upload(y, ny, &h->mem[1])) != cudaSuccess ||
-      (e = upload(depth, depth_len, &h->mem[2])) != cudaSuccess) {
-    free_mem(h->mem, 4);
+  if ((e = upload(x, nx, &h->mem, &h->dev.x)) != cudaSuccess ||
+      (e = upload(y, ny, &h->mem, &h->dev.y)) != cudaSuccess ||
+      (e = upload(depth, depth_len, &h->mem, &h->dev.depth)) != cudaSuccess ||
+      (e = upload(d32.data(), depth_len, &h->mem, &h->dev.depth32)) != cudaSuccess ||
+      (e = upload(gx.data(), depth_len, &h->mem, &h->dev.gx)) != cudaSuccess ||
+      (e = upload(gy.data(), depth_len, &h->mem, &h->dev.gy)) != cudaSuccess) {
+    free_mem(h->mem);
     delete h;
     return cuda_fail(e, "staging bathymetry grid");
   }
-  h->dev.x = static_cast<const float *>(h->mem[0]);
-  h->dev.y = static_cast<const float *>(h->mem[1]);
-  h->dev.depth = static_cast<const double *>(h->mem[2]);
   h->dev.depth_len = depth_len;
-  fill_bathy_grid_scalars(h, x, y, nx, ny);
   *out = h;
   return MR_OK;
 }
@@ -207,20 +229,7 @@ int make_current_grid(size_t nx, size_t ny, const double *x, const double *y, co
   mr_current *h = new mr_current();
   h->dev.kind = mr::CURRENT_GRID;
   h->device = device;
-  cudaError_t e;
-  if ((e = upload(x, nx, &h->mem[0])) != cudaSuccess ||
-      (e = upload(y, ny, &h->mem[1])) != cudaSuccess ||
-      (e = upload(u, u_len, &h->mem[2])) != cudaSuccess ||
-      (e = upload(v, v_len, &h->mem[3])) != cudaSuccess) {
-    free_mem(h->mem, 4);
-    delete h;
-    return cuda_fail(e, "staging current grid");
-  }
   mr::CurrentDev &d = h->dev;
-  d.x = static_cast<const double *>(h->mem[0]);
-  d.y = static_cast<const double *>(h->mem[1]);
-  d.u = static_cast<const double *>(h->mem[2]);
-  d.v = static_cast<const double *>(h->mem[3]);
   d.u_len = u_len;
   d.v_len = v_len;
   d.nx = nx;
@@ -237,13 +246,51 @@ int make_current_grid(size_t nx, size_t ny, const double *x, const double *y, co
     d.xspace = x[1] - x[0];
     d.yspace = y[1] - y[0];
   }
+  // Tables (fields.h): axes and values as f32 (interpolate, :375-396) and
+  // the f64 cell gradients of :522-536.
+  const size_t len = u_len < v_len ? u_len : v_len;
+  std::vector<float> x32(nx), y32(ny), u32(u_len), v32(v_len);
+  std::vector<double> dudx(len, 0.0), dudy(len, 0.0), dvdx(len, 0.0), dvdy(len, 0.0);
+  for (size_t i = 0; i < nx; ++i) x32[i] = static_cast<float>(x[i]);
+  for (size_t i = 0; i < ny; ++i) y32[i] = static_cast<float>(y[i]);
+  for (size_t i = 0; i < u_len; ++i) u32[i] = static_cast<float>(u[i]);
+  for (size_t i = 0; i < v_len; ++i) v32[i] = static_cast<float>(v[i]);
+  if (!h->one_point_axis) {
+    for (size_t j = 0; j + 1 < ny; ++j) {
+      for (size_t i = 0; i + 1 < nx; ++i) {
+        const size_t sw = nx * j + i;
+        if (nx * (j + 1) + i + 1 >= len) continue;
+        dudx[sw] = (u[sw + 1] - u[sw]) / d.xspace;
+        dudy[sw] = (u[sw + nx] - u[sw]) / d.yspace;
+        dvdx[sw] = (v[sw + 1] - v[sw]) / d.xspace;
+        dvdy[sw] = (v[sw + nx] - v[sw]) / d.yspace;
+      }
+    }
+  }
+  cudaError_t e;
+  if ((e = upload(x, nx, &h->mem, &d.x)) != cudaSuccess ||
+      (e = upload(y, ny, &h->mem, &d.y)) != cudaSuccess ||
+      (e = upload(u, u_len, &h->mem, &d.u)) != cudaSuccess ||
+      (e = upload(v, v_len, &h->mem, &d.v)) != cudaSuccess ||
+      (e = upload(x32.data(), nx, &h->mem, &d.x32)) != cudaSuccess ||
+      (e = upload(y32.data(), ny, &h->mem, &d.y32)) != cudaSuccess ||
+      (e = upload(u32.data(), u_len, &h->mem, &d.u32)) != cudaSuccess ||
+      (e = upload(v32.data(), v_len, &h->mem, &d.v32)) != cudaSuccess ||
+      (e = upload(dudx.data(), len, &h->mem, &d.dudx)) != cudaSuccess ||
+      (e = upload(dudy.data(), len, &h->mem, &d.dudy)) != cudaSuccess ||
+      (e = upload(dvdx.data(), len, &h->mem, &d.dvdx)) != cudaSuccess ||
+      (e = upload(dvdy.data(), len, &h->mem, &d.dvdy)) != cudaSuccess) {
+    free_mem(h->mem);
+    delete h;
+    return cuda_fail(e, "staging current grid");
+  }
   *out = h;
   return MR_OK;
 }
 
 int launch(const mr_bathymetry *b, const mr_current *c, size_t n, const double *x0,
            const double *y0, const double *kx0, const double *ky0, double t0, double dt,
-           uint64_t nsteps, int stop_rule, size_t rows_cap, double *traj, int32_t *n_rows,
+           uint64_t nsteps, int options, size_t rows_cap, double *traj, int32_t *n_rows,
            uint8_t *status, cudaStream_t stream) {
   mr::TraceArgs a;
   a.n = n;
@@ -255,7 +302,8 @@ int launch(const mr_bathymetry *b, const mr_current *c, size_t n, const double *
   a.traj = traj;
   a.n_rows = n_rows;
   a.status = status;
-  cudaError_t e = mr::launch_rk4_f64(b->dev, c->dev, a, stop_rule, stream);
+  cudaError_t e = mr::launch_rk4_f64(b->dev, c->dev, a, options & MR_STOP_FRESH,
+                                     (options & MR_MATH_IDENTITY) != 0, stream);
   if (e != cudaSuccess) return cuda_fail(e, "rk4_f64 launch");
   return MR_OK;
 }
@@ -327,12 +375,12 @@ int mr_bathymetry_array(size_t n, const float *arr, mr_bathymetry **out) {
   b->device = device;
   b->dev.kind = mr::BATHY_ARRAY;
   b->dev.an = n;
-  cudaError_t e = upload(arr, n * n, &b->mem[0]);
+  cudaError_t e = upload(arr, n * n, &b->mem, &b->dev.arr);
   if (e != cudaSuccess) {
+    free_mem(b->mem);
     delete b;
     return cuda_fail(e, "staging array depth");
   }
-  b->dev.arr = static_cast<const float *>(b->mem[0]);
   *out = b;
   return MR_OK;
 }
@@ -340,7 +388,7 @@ int mr_bathymetry_array(size_t n, const float *arr, mr_bathymetry **out) {
 void mr_bathymetry_destroy(mr_bathymetry *b) {
   if (!b) return;
   DeviceGuard g(b->device);
-  free_mem(b->mem, 4);
+  free_mem(b->mem);
   delete b;
 }
 
@@ -380,32 +428,32 @@ int mr_current_constant(double u, double v, mr_current **out) {
 void mr_current_destroy(mr_current *c) {
   if (!c) return;
   DeviceGuard g(c->device);
-  free_mem(c->mem, 4);
+  free_mem(c->mem);
   delete c;
 }
 
 int mr_trace_device(const mr_bathymetry *b, const mr_current *c, size_t n, const double *x0,
                     const double *y0, const double *kx0, const double *ky0, double t0,
-                    double t_end, double dt, int stop_rule, size_t rows_cap, double *traj,
+                    double t_end, double dt, int options, size_t rows_cap, double *traj,
                     int32_t *n_rows, uint8_t *status, void *stream) {
   uint64_t nsteps = 0;
-  int rc = check_trace_args(b, c, n, x0, y0, kx0, ky0, t0, t_end, dt, stop_rule, rows_cap, traj,
+  int rc = check_trace_args(b, c, n, x0, y0, kx0, ky0, t0, t_end, dt, options, rows_cap, traj,
                             n_rows, status, &nsteps);
   if (rc) return rc;
   if (n == 0) return MR_OK;
   DeviceGuard g(b->device);
   if (!g.ok()) return fail(MR_ERR_CUDA, "cannot select device %d", b->device);
   cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : cudaStreamPerThread;
-  return launch(b, c, n, x0, y0, kx0, ky0, t0, dt, nsteps, stop_rule, rows_cap, traj, n_rows,
+  return launch(b, c, n, x0, y0, kx0, ky0, t0, dt, nsteps, options, rows_cap, traj, n_rows,
                 status, s);
 }
 
 int mr_trace(const mr_bathymetry *b, const mr_current *c, size_t n, const double *x0,
              const double *y0, const double *kx0, const double *ky0, double t0, double t_end,
-             double dt, int stop_rule, size_t rows_cap, double *traj, int32_t *n_rows,
+             double dt, int options, size_t rows_cap, double *traj, int32_t *n_rows,
              uint8_t *status) {
   uint64_t nsteps = 0;
-  int rc = check_trace_args(b, c, n, x0, y0, kx0, ky0, t0, t_end, dt, stop_rule, rows_cap, traj,
+  int rc = check_trace_args(b, c, n, x0, y0, kx0, ky0, t0, t_end, dt, options, rows_cap, traj,
                             n_rows, status, &nsteps);
   if (rc) return rc;
   if (n == 0) return MR_OK;
@@ -438,7 +486,7 @@ int mr_trace(const mr_bathymetry *b, const mr_current *c, size_t n, const double
     e = cudaMallocAsync(reinterpret_cast<void **>(&d_rows), n * sizeof(int32_t), s);
   if (e == cudaSuccess && own_status) e = cudaMallocAsync(reinterpret_cast<void **>(&d_status), n, s);
   if (e == cudaSuccess) {
-    rc = launch(b, c, n, d_in, d_in + n, d_in + 2 * n, d_in + 3 * n, t0, dt, nsteps, stop_rule,
+    rc = launch(b, c, n, d_in, d_in + n, d_in + 2 * n, d_in + 3 * n, t0, dt, nsteps, options,
                 rows_cap, d_traj, d_rows, d_status, s);
   } else {
     rc = cuda_fail(e, "allocating device output buffers");
@@ -464,7 +512,7 @@ int mr_single_ray(const mr_bathymetry *b, const mr_current *c, double x0, double
   if (!rows || !n_rows) return fail(MR_ERR_INVALID_ARGUMENT, "null output");
   std::vector<double> traj(5 * rows_cap);
   uint8_t status = 0;
-  int rc = mr_trace(b, c, 1, &x0, &y0, &kx0, &ky0, 0.0, duration, step_size, MR_STOP_STAGE1,
+  int rc = mr_trace(b, c, 1, &x0, &y0, &kx0, &ky0, 0.0, duration, step_size, kDropInOptions,
                     rows_cap, traj.data(), n_rows, &status);
   if (rc) return rc;
   for (size_t r = 0; r < rows_cap; ++r)
@@ -494,7 +542,7 @@ int mr_ray_tracing_files(const char *bathymetry_path, const char *current_path, 
   int rc = mr_bathymetry_open(bathymetry_path, "x", "y", "depth", &b);
   if (!rc) rc = mr_current_open(current_path, "x", "y", "u", "v", &c);
   if (!rc)
-    rc = mr_trace(b, c, n, x0, y0, kx0, ky0, 0.0, duration, step_size, MR_STOP_STAGE1, rows_cap,
+    rc = mr_trace(b, c, n, x0, y0, kx0, ky0, 0.0, duration, step_size, kDropInOptions, rows_cap,
                   traj, n_rows, status);
   mr_bathymetry_destroy(b);
   mr_current_destroy(c);

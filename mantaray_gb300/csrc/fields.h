@@ -1,12 +1,20 @@
 // fields.h -- device-side descriptions of the bathymetry and current fields.
 //
 // Plain structs passed by value as kernel parameters.  Grid arrays live in
-// device memory (HBM) in the reference's own precisions and flat layout
-// (src/bathymetry/cartesian_netcdf3.rs:35-43: f32 axes + f64 depth;
-// src/current/cartesian_current.rs:18-27: f64 axes, u, v), flat index
-// nx*j + i (cartesian_netcdf3.rs:465-471, cartesian_current.rs:421-427).
-// Host-precomputed scalars repeat the reference's own per-call arithmetic
-// (same operands, same precision), so they are bit-identical to it.
+// device memory (HBM) with the reference's flat layout, index nx*j + i
+// (src/bathymetry/cartesian_netcdf3.rs:465-471,
+// src/current/cartesian_current.rs:421-427).  Besides the reference's own
+// arrays (f32 axes + f64 depth; f64 axes, u, v) a handle holds tables derived
+// from them once, on the host, with the reference's own operations, so a
+// lookup reads the values it needs instead of recomputing them per call:
+//  - f32 copies of every value the reference casts to f32 before bilinear
+//    interpolation (depth, u, v, current axes: `as f32`, round to nearest);
+//  - per-cell forward differences, indexed by the cell's south-west corner:
+//    bathymetry (d[j][i+1] - d[j][i]) / x_space cast to f32 and
+//    (d[j+1][i] - d[j][i]) / y_space cast to f32 (cartesian_netcdf3.rs:119-134),
+//    current du/dx, du/dy, dv/dx, dv/dy in f64 (cartesian_current.rs:515-536).
+// Each table entry is bit-identical to the value the reference computes at
+// lookup time.
 #pragma once
 
 #include <stdint.h>
@@ -28,9 +36,12 @@ enum CurrentKind : int {
 struct BathyDev {
   int kind;
   uint64_t nx, ny;
-  const float *x;        // [nx]
+  const float *x;        // [nx] axis (f32, as the reference stores it)
   const float *y;        // [ny]
-  const double *depth;   // [depth_len], flat nx*j + i
+  const double *depth;   // [depth_len] f64 depth, flat nx*j + i
+  const float *depth32;  // [depth_len] depth as f32
+  const float *gx;       // [depth_len] f32 cell gradient d/dx, by south-west corner
+  const float *gy;       // [depth_len] f32 cell gradient d/dy
   uint64_t depth_len;
   // nearest(): spacing = |a[1] - a[0]| (f32), high = (n - 1) as f32
   float x0, xsp, xhigh;
@@ -47,10 +58,15 @@ struct BathyDev {
 struct CurrentDev {
   int kind;
   uint64_t nx, ny;
-  const double *x;   // [nx]
+  const double *x;   // [nx] f64 axes
   const double *y;   // [ny]
-  const double *u;   // [u_len]
+  const double *u;   // [u_len] f64 values
   const double *v;   // [v_len]
+  const float *x32;  // [nx] axes as f32
+  const float *y32;  // [ny]
+  const float *u32;  // [u_len] values as f32
+  const float *v32;  // [v_len]
+  const double *dudx, *dudy, *dvdx, *dvdy;  // [min(u_len, v_len)] cell gradients
   uint64_t u_len, v_len;
   double x0, xsp, xhigh;   // nearest() in f64
   double y0, ysp, yhigh;

@@ -24,6 +24,6 @@ struct TraceArgs {
 };
 
 cudaError_t launch_rk4_f64(const BathyDev &b, const CurrentDev &c, const TraceArgs &a,
-                           int stop_rule, cudaStream_t stream);
+                           int stop_rule, int identity_math, cudaStream_t stream);
 
 }  // namespace mr

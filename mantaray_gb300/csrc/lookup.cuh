@@ -1,0 +1,209 @@
+// lookup.cuh -- field lookups of the reference, bit for bit, on the GPU.
+//
+// depth_and_gradient (src/bathymetry/cartesian_netcdf3.rs:98-135 and the
+// analytic fields) and current_and_gradient
+// (src/current/cartesian_current.rs:487-542).  Index arithmetic, corner
+// rules, the coincident-corner shortcut and the f32 bilinear form follow the
+// reference operation for operation; values and cell gradients come from the
+// handle's tables (fields.h), which hold exactly what the reference computes.
+// Translation units including this file are compiled with -fmad=false.
+#pragma once
+
+#include <math.h>
+#include <stdint.h>
+
+#include "fields.h"
+
+namespace mr {
+
+// Rust `v as usize`: saturating, NaN -> 0.
+__device__ __forceinline__ uint64_t as_usize(float v) {
+  if (!(v > 0.0f)) return 0ull;
+  if (v >= 18446744073709551616.0f) return ~0ull;
+  return static_cast<uint64_t>(v);
+}
+__device__ __forceinline__ uint64_t as_usize(double v) {
+  if (!(v > 0.0)) return 0ull;
+  if (v >= 18446744073709551616.0) return ~0ull;
+  return static_cast<uint64_t>(v);
+}
+__device__ __forceinline__ float rfract(float v) { return v - truncf(v); }
+__device__ __forceinline__ double rfract(double v) { return v - trunc(v); }
+__device__ __forceinline__ float rround(float v) { return roundf(v); }
+__device__ __forceinline__ double rround(double v) { return round(v); }
+__device__ __forceinline__ float rfloor(float v) { return floorf(v); }
+__device__ __forceinline__ double rfloor(double v) { return floor(v); }
+__device__ __forceinline__ float rceil(float v) { return ceilf(v); }
+__device__ __forceinline__ double rceil(double v) { return ceil(v); }
+
+__device__ __forceinline__ float f32_nan() { return __int_as_float(0x7fffffff); }
+__device__ __forceinline__ double f64_nan() { return __longlong_as_double(0x7ff8000000000000ll); }
+
+// interpolator::bilinear, src/interpolator.rs:39-84.  Corners in the order
+// [(x1,y1), (x1,y2), (x2,y2), (x2,y1)] given as px/py/pv.
+__device__ __forceinline__ int bilinear_exact(const float px[4], const float py[4],
+                                              const float pv[4], float tx, float ty,
+                                              float *out) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    if (tx == px[i] && ty == py[i]) {  // :46-50 coincident corner
+      *out = pv[i];
+      return RHS_OK;
+    }
+  }
+  const float bt0 = px[1] - px[0], bt1 = py[1] - py[0];
+  const float dt0 = px[3] - px[0], dt1 = py[3] - py[0];
+  const float tt0 = tx - px[0], tt1 = ty - py[0];
+  const float det = bt0 * dt1 - dt0 * bt1;  // :64
+  if (det == 0.0f) return RHS_INVALID_ARGUMENT;
+  const float m00 = dt1 / det;
+  const float m01 = -(dt0 / det);
+  const float m10 = -(bt1 / det);
+  const float m11 = bt0 / det;
+  const float x = m00 * tt0 + m01 * tt1;  // :74
+  const float y = m10 * tt0 + m11 * tt1;  // :75
+  const float a00 = pv[0];
+  const float a10 = pv[1] - pv[0];
+  const float a01 = pv[3] - pv[0];
+  const float a11 = pv[2] - pv[0] - a10 - a01;
+  *out = a00 + a10 * x + a01 * y + a11 * x * y;  // :83, left to right
+  return RHS_OK;
+}
+
+// nearest + the edge/on-grid/interior corner rule (cartesian_netcdf3.rs:274-390
+// in f32, cartesian_current.rs:231-339 in f64).  a0/sp/high are the host
+// precomputed a[0], |a[1]-a[0]| and (n-1) as T; n >= 2.
+template <typename T>
+__device__ __forceinline__ int corner_pair(T target, T a0, T sp, T high, uint64_t *lo,
+                                           uint64_t *hi) {
+  const T idx = (target - a0) / sp;
+  if (idx < T(0) || idx > high) return RHS_INDEX_OUT_OF_BOUNDS;
+  if (idx == T(0)) {
+    *lo = as_usize(idx);
+    *hi = *lo + 1;
+  } else if (idx == high) {
+    *lo = as_usize(idx) - 1;
+    *hi = as_usize(idx);
+  } else if (rfract(idx) == T(0)) {
+    *lo = as_usize(rround(idx));
+    *hi = *lo + 1;
+  } else {
+    *lo = as_usize(rfloor(idx));
+    *hi = as_usize(rceil(idx));
+  }
+  return RHS_OK;
+}
+
+// BathymetryData::depth_and_gradient for every kind.  out = (h, dh/dx, dh/dy).
+__device__ __forceinline__ int depth_and_gradient(const BathyDev &b, float x, float y,
+                                                  float out[3]) {
+  if (b.kind == BATHY_GRID) {
+    // cartesian_netcdf3.rs:98-135
+    if (isnan(x) || isnan(y)) {
+      out[0] = out[1] = out[2] = f32_nan();
+      return RHS_OK;
+    }
+    uint64_t x1, x2, y1, y2;
+    int e = corner_pair<float>(x, b.x0, b.xsp, b.xhigh, &x1, &x2);
+    if (e) return e;
+    e = corner_pair<float>(y, b.y0, b.ysp, b.yhigh, &y1, &y2);
+    if (e) return e;
+    // depth_at_indexes checks every corner's flat index against the array
+    // length (:465-471); the largest of them is nx*y2 + x2.
+    const uint64_t sw = b.nx * y1 + x1, nw = b.nx * y2 + x1;
+    const uint64_t ne = b.nx * y2 + x2, se = b.nx * y1 + x2;
+    if (ne >= b.depth_len) return RHS_INDEX_OUT_OF_BOUNDS;
+    const float ax1 = __ldg(b.x + x1), ax2 = __ldg(b.x + x2);
+    const float ay1 = __ldg(b.y + y1), ay2 = __ldg(b.y + y2);
+    const float px[4] = {ax1, ax1, ax2, ax2};
+    const float py[4] = {ay1, ay2, ay2, ay1};
+    const float pv[4] = {__ldg(b.depth32 + sw), __ldg(b.depth32 + nw), __ldg(b.depth32 + ne),
+                         __ldg(b.depth32 + se)};
+    float depth;
+    e = bilinear_exact(px, py, pv, x, y, &depth);
+    if (e) return e;
+    out[0] = depth;
+    if (x2 == x1 + 1 && y2 == y1 + 1) {
+      out[1] = __ldg(b.gx + sw);
+      out[2] = __ldg(b.gy + sw);
+    } else {  // degenerate corners (NaN index): the reference's own expression
+      const double d_sw = __ldg(b.depth + sw);
+      out[1] = __double2float_rn((__ldg(b.depth + se) - d_sw) / b.xspace);
+      out[2] = __double2float_rn((__ldg(b.depth + nw) - d_sw) / b.yspace);
+    }
+    return RHS_OK;
+  }
+  if (b.kind == BATHY_CONSTANT) {
+    if (isnan(x) || isnan(y)) {
+      out[0] = out[1] = out[2] = f32_nan();
+    } else {
+      out[0] = b.h; out[1] = 0.0f; out[2] = 0.0f;
+    }
+    return RHS_OK;
+  }
+  if (b.kind == BATHY_SLOPE) {
+    if (isnan(x) || isnan(y)) {
+      out[0] = out[1] = out[2] = f32_nan();
+    } else {
+      out[0] = b.s_h0 + b.s_dhdx * (x - b.s_x0) + b.s_dhdy * (y - b.s_y0);
+      out[1] = b.s_dhdx;
+      out[2] = b.s_dhdy;
+    }
+    return RHS_OK;
+  }
+  // BATHY_ARRAY
+  const uint64_t i = as_usize(x), j = as_usize(y);
+  if (i >= b.an || j >= b.an) {
+    out[0] = out[1] = out[2] = f32_nan();
+  } else {
+    out[0] = __ldg(b.arr + i * b.an + j); out[1] = 0.0f; out[2] = 0.0f;
+  }
+  return RHS_OK;
+}
+
+// CurrentData::current_and_gradient.  out = (u, v, du/dx, du/dy, dv/dx, dv/dy).
+__device__ __forceinline__ int current_and_gradient(const CurrentDev &c, double x, double y,
+                                                    double out[6]) {
+  if (c.kind == CURRENT_CONSTANT) {
+    out[0] = c.cu; out[1] = c.cv;
+    out[2] = out[3] = out[4] = out[5] = 0.0;
+    return RHS_OK;
+  }
+  // cartesian_current.rs:487-542
+  uint64_t x1, x2, y1, y2;
+  int e = corner_pair<double>(x, c.x0, c.xsp, c.xhigh, &x1, &x2);
+  if (e) return e;
+  e = corner_pair<double>(y, c.y0, c.ysp, c.yhigh, &y1, &y2);
+  if (e) return e;
+  const uint64_t sw = c.nx * y1 + x1, nw = c.nx * y2 + x1;
+  const uint64_t ne = c.nx * y2 + x2, se = c.nx * y1 + x2;
+  // val_from_arr (:421-427) on u, then v: the largest flat index is ne.
+  if (ne >= c.u_len || ne >= c.v_len) return RHS_INDEX_OUT_OF_BOUNDS;
+  const float ax1 = __ldg(c.x32 + x1), ax2 = __ldg(c.x32 + x2);
+  const float ay1 = __ldg(c.y32 + y1), ay2 = __ldg(c.y32 + y2);
+  const float px[4] = {ax1, ax1, ax2, ax2};
+  const float py[4] = {ay1, ay2, ay2, ay1};
+  const float tx = __double2float_rn(x), ty = __double2float_rn(y);
+  const float pu[4] = {__ldg(c.u32 + sw), __ldg(c.u32 + nw), __ldg(c.u32 + ne), __ldg(c.u32 + se)};
+  const float pv[4] = {__ldg(c.v32 + sw), __ldg(c.v32 + nw), __ldg(c.v32 + ne), __ldg(c.v32 + se)};
+  float u, v;
+  if ((e = bilinear_exact(px, py, pu, tx, ty, &u))) return e;
+  if ((e = bilinear_exact(px, py, pv, tx, ty, &v))) return e;
+  out[0] = static_cast<double>(u);
+  out[1] = static_cast<double>(v);
+  if (x2 == x1 + 1 && y2 == y1 + 1) {
+    out[2] = __ldg(c.dudx + sw);
+    out[3] = __ldg(c.dudy + sw);
+    out[4] = __ldg(c.dvdx + sw);
+    out[5] = __ldg(c.dvdy + sw);
+  } else {
+    const double u_sw = __ldg(c.u + sw), v_sw = __ldg(c.v + sw);
+    out[2] = (__ldg(c.u + se) - u_sw) / c.xspace;
+    out[3] = (__ldg(c.u + nw) - u_sw) / c.yspace;
+    out[4] = (__ldg(c.v + se) - v_sw) / c.xspace;
+    out[5] = (__ldg(c.v + nw) - v_sw) / c.yspace;
+  }
+  return RHS_OK;
+}
+
+}  // namespace mr

@@ -9,7 +9,10 @@
 // consecutive doubles per variable (fully coalesced 256-byte rows).  Rows after
 // a ray's last row are NaN, as the Python wrapper pads them.
 //
-// Compiled with -fmad=false: no contraction anywhere in this file.
+// The right-hand side is a template parameter (RhsLibm: the reference's
+// transcendental calls; RhsIdentity: the same quantities from fewer FP64
+// instructions, see ray_exact.cuh).  Compiled with -fmad=false: no
+// contraction anywhere in this file.
 
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -40,7 +43,7 @@ __device__ __forceinline__ void store_nan_row(double *traj, uint64_t plane, uint
   for (int v = 0; v < 5; ++v) p[v * plane] = nan;
 }
 
-template <int STOP_RULE>
+template <int STOP_RULE, typename Rhs>
 __global__ void __launch_bounds__(kK1Block) rk4_f64_kernel(BathyDev b, CurrentDev c,
                                                            TraceArgs a) {
   const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -55,7 +58,7 @@ __global__ void __launch_bounds__(kK1Block) rk4_f64_kernel(BathyDev b, CurrentDe
     y[0] = a.x0[i]; y[1] = a.y0[i]; y[2] = a.kx0[i]; y[3] = a.ky0[i];
     store_row(a.traj, plane, a.n, 0, i, t, y);
     rows = 1;
-    system_exact(b, c, y, k1);
+    system<Rhs>(b, c, y, k1);
   }
   const double half = a.dt / 2.0;
   const double sixth = a.dt / 6.0;
@@ -67,13 +70,13 @@ __global__ void __launch_bounds__(kK1Block) rk4_f64_kernel(BathyDev b, CurrentDe
       double k2[4], k3[4], k4[4], tmp[4];
 #pragma unroll
       for (int q = 0; q < 4; ++q) tmp[q] = y[q] + k1[q] * half;
-      system_exact(b, c, tmp, k2);
+      system<Rhs>(b, c, tmp, k2);
 #pragma unroll
       for (int q = 0; q < 4; ++q) tmp[q] = y[q] + k2[q] * half;
-      system_exact(b, c, tmp, k3);
+      system<Rhs>(b, c, tmp, k3);
 #pragma unroll
       for (int q = 0; q < 4; ++q) tmp[q] = y[q] + k3[q] * a.dt;
-      system_exact(b, c, tmp, k4);
+      system<Rhs>(b, c, tmp, k4);
       double yn[4];
 #pragma unroll
       for (int q = 0; q < 4; ++q) yn[q] = y[q] + (k1[q] + k2[q] * 2.0 + k3[q] * 2.0 + k4[q]) * sixth;
@@ -83,7 +86,7 @@ __global__ void __launch_bounds__(kK1Block) rk4_f64_kernel(BathyDev b, CurrentDe
       // The next step's first stage doubles as the FRESH stop-rule derivative
       // (system() does not depend on t).
       double fresh[4];
-      system_exact(b, c, yn, fresh);
+      system<Rhs>(b, c, yn, fresh);
       const bool stop = STOP_RULE == 1 ? (all_nan4(fresh) || all_nan4(yn))
                                        : (all_nan4(k1) || all_nan4(yn));
 #pragma unroll
@@ -104,13 +107,20 @@ __global__ void __launch_bounds__(kK1Block) rk4_f64_kernel(BathyDev b, CurrentDe
 }  // namespace
 
 cudaError_t launch_rk4_f64(const BathyDev &b, const CurrentDev &c, const TraceArgs &a,
-                           int stop_rule, cudaStream_t stream) {
+                           int stop_rule, int identity_math, cudaStream_t stream) {
   if (a.n == 0) return cudaSuccess;
   const unsigned grid = static_cast<unsigned>((a.n + kK1Block - 1) / kK1Block);
-  if (stop_rule == 1)
-    rk4_f64_kernel<1><<<grid, kK1Block, 0, stream>>>(b, c, a);
-  else
-    rk4_f64_kernel<0><<<grid, kK1Block, 0, stream>>>(b, c, a);
+  if (identity_math) {
+    if (stop_rule == 1)
+      rk4_f64_kernel<1, RhsIdentity><<<grid, kK1Block, 0, stream>>>(b, c, a);
+    else
+      rk4_f64_kernel<0, RhsIdentity><<<grid, kK1Block, 0, stream>>>(b, c, a);
+  } else {
+    if (stop_rule == 1)
+      rk4_f64_kernel<1, RhsLibm><<<grid, kK1Block, 0, stream>>>(b, c, a);
+    else
+      rk4_f64_kernel<0, RhsLibm><<<grid, kK1Block, 0, stream>>>(b, c, a);
+  }
   return cudaGetLastError();
 }
 

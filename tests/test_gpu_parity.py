@@ -21,6 +21,15 @@ pytestmark = pytest.mark.gpu
 
 RTOL = 1e-9
 F64_EPS = np.finfo(np.float64).eps
+MATH = "libm"
+
+
+@pytest.fixture(autouse=True, params=["libm", "identity"])
+def math_mode(request):
+    """Every parity test runs for both right-hand-side arithmetic options."""
+    global MATH
+    MATH = request.param
+    yield request.param
 
 
 @pytest.fixture(scope="module")
@@ -36,7 +45,7 @@ def both(mr, oracle, bathy, current, x0, y0, kx0, ky0, t0, t_end, dt, stop_rule=
     for the same field description.  bathy/current: ("constant", h) etc."""
     gb, ob = make_bathy(mr, oracle, bathy)
     gc, oc = make_current(mr, oracle, current)
-    g = mr.trace(gb, gc, x0, y0, kx0, ky0, t_end - t0, dt, t0=t0, stop_rule=stop_rule)
+    g = mr.trace(gb, gc, x0, y0, kx0, ky0, t_end - t0, dt, t0=t0, stop_rule=stop_rule, math=MATH)
     o = oracle.trace(ob, oc, x0, y0, kx0, ky0, t0, t_end, dt, stop_rule=stop_rule)
     return g.traj, g.n_rows, g.status, o[0], o[1], o[2]
 
@@ -265,13 +274,13 @@ def test_seamount_full_size_properties(mr, oracle):
     traj = torch.empty((5, rows, w.n), dtype=torch.float64, device=dev)
     n_rows = torch.empty(w.n, dtype=torch.int32, device=dev)
     status = torch.empty(w.n, dtype=torch.uint8, device=dev)
-    mr.trace_device(b, c, *ins, w.t0, w.t_end, w.dt, traj, n_rows, status)
+    mr.trace_device(b, c, *ins, w.t0, w.t_end, w.dt, traj, n_rows, status, math=MATH)
     torch.cuda.synchronize()
     checksum1 = torch.nansum(traj[1:], dim=(1, 2)).cpu().numpy()
     rows1 = n_rows.cpu().numpy()
     # determinism: a second run is bitwise identical
     traj2 = torch.empty_like(traj)
-    mr.trace_device(b, c, *ins, w.t0, w.t_end, w.dt, traj2, n_rows, status)
+    mr.trace_device(b, c, *ins, w.t0, w.t_end, w.dt, traj2, n_rows, status, math=MATH)
     torch.cuda.synchronize()
     assert torch.equal(torch.nan_to_num(traj, nan=-1e300), torch.nan_to_num(traj2, nan=-1e300))
     del traj2
