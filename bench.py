@@ -40,9 +40,10 @@ L2_FLUSH_BYTES = 512 << 20  # > 129 MB L2
 GRID_BYTES_PER_RAY_STEP = 4 * 3 * 4 * 8
 OUT_BYTES_PER_ROW = 5 * 8
 # FP64 floating-point operations one ray-step executes (DADD/DMUL = 1,
-# DFMA = 2), counted by ncu on the plain kernel over the seamount workload
+# DFMA = 2), per right-hand-side arithmetic, counted by ncu on the plain
+# kernel over the seamount workload
 # (sm__sass_thread_inst_executed_op_d{add,mul,fma}_pred_on; profiles/).
-FP64_FLOP_PER_RAY_STEP = None
+FP64_FLOP_PER_RAY_STEP = {"libm": None, "identity": None}
 
 
 def parse():
@@ -323,12 +324,13 @@ def gb300_arm(args, rank: int, world: int, local_rank: int):
     except (OSError, ValueError):
         pass
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    if FP64_FLOP_PER_RAY_STEP:
-        fp64_achieved = rs_per_s_kernel * FP64_FLOP_PER_RAY_STEP / 1e12
+    flop_per_rs = FP64_FLOP_PER_RAY_STEP.get(args.math)
+    if flop_per_rs:
+        fp64_achieved = rs_per_s_kernel * flop_per_rs / 1e12
         roofline = {"bound": "fp64", "achieved": fp64_achieved, "peak": fp64_peak.value,
                     "unit": "TFLOP/s", "frac": fp64_achieved / fp64_peak.value,
                     "peak_source": "measured: FP64 FMA-chain kernel on this GPU, this run",
-                    "flop_per_ray_step": FP64_FLOP_PER_RAY_STEP}
+                    "flop_per_ray_step": flop_per_rs}
     else:
         roofline = {"bound": "fp64", "achieved": None, "peak": fp64_peak.value,
                     "unit": "TFLOP/s", "frac": None,

@@ -245,6 +245,8 @@ int make_current_grid(size_t nx, size_t ny, const double *x, const double *y, co
     d.yhigh = static_cast<double>(ny - 1);
     d.xspace = x[1] - x[0];
     d.yspace = y[1] - y[0];
+    d.inv_xsp = 1.0 / d.xsp;
+    d.inv_ysp = 1.0 / d.ysp;
   }
   // Tables (fields.h): axes and values as f32 (interpolate, :375-396) and
   // the f64 cell gradients of :522-536.

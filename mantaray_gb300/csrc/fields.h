@@ -70,6 +70,7 @@ struct CurrentDev {
   uint64_t u_len, v_len;
   double x0, xsp, xhigh;   // nearest() in f64
   double y0, ysp, yhigh;
+  double inv_xsp, inv_ysp; // 1 / spacing (fast path of the index, lookup.cuh)
   double xspace, yspace;   // a[1] - a[0] (cartesian_current.rs:515-516)
   double cu, cv;           // constant current
 };

@@ -94,6 +94,29 @@ __device__ __forceinline__ int corner_pair(T target, T a0, T sp, T high, uint64_
   return RHS_OK;
 }
 
+// corner_pair<double> with the division replaced by a multiplication where
+// that provably gives the same answer.  q = (target - a0) * (1/sp) lies within
+// two ulps of the reference's idx = (target - a0) / sp.  When q is more than a
+// few ulps away from every integer, idx has the same floor, is not an integer,
+// and lies on the same side of 0 and of high, so the corner pair follows from
+// floor(q) alone; otherwise (grid lines, NaN, infinities) the exact rule runs.
+__device__ __forceinline__ int corner_pair_f64(double target, double a0, double sp,
+                                               double inv_sp, double high, uint64_t *lo,
+                                               uint64_t *hi) {
+  const double a = target - a0;
+  const double q = a * inv_sp;
+  const double n = floor(q);
+  const double fr = q - n;  // exact for |q| < 2^52
+  const double tol = fabs(q) * 0x1p-48 + 0x1p-1000;
+  if (fr > tol && fr < 1.0 - tol) {
+    if (n < 0.0 || n >= high) return RHS_INDEX_OUT_OF_BOUNDS;
+    *lo = static_cast<uint64_t>(n);
+    *hi = *lo + 1;
+    return RHS_OK;
+  }
+  return corner_pair<double>(target, a0, sp, high, lo, hi);
+}
+
 // BathymetryData::depth_and_gradient for every kind.  out = (h, dh/dx, dh/dy).
 __device__ __forceinline__ int depth_and_gradient(const BathyDev &b, float x, float y,
                                                   float out[3]) {
@@ -171,9 +194,9 @@ __device__ __forceinline__ int current_and_gradient(const CurrentDev &c, double 
   }
   // cartesian_current.rs:487-542
   uint64_t x1, x2, y1, y2;
-  int e = corner_pair<double>(x, c.x0, c.xsp, c.xhigh, &x1, &x2);
+  int e = corner_pair_f64(x, c.x0, c.xsp, c.inv_xsp, c.xhigh, &x1, &x2);
   if (e) return e;
-  e = corner_pair<double>(y, c.y0, c.ysp, c.yhigh, &y1, &y2);
+  e = corner_pair_f64(y, c.y0, c.ysp, c.inv_ysp, c.yhigh, &y1, &y2);
   if (e) return e;
   const uint64_t sw = c.nx * y1 + x1, nw = c.nx * y2 + x1;
   const uint64_t ne = c.nx * y2 + x2, se = c.nx * y1 + x2;

@@ -72,16 +72,18 @@ struct RhsIdentity {
     double cur[6];
     e = current_and_gradient(c, x, y, cur);
     if (e) return e;
-    const double k = sqrt(kx * kx + ky * ky);
-    if (!(h <= 0.0) && k <= 0.0) return RHS_ARGUMENT_OUT_OF_BOUNDS;  // group_velocity's Err
-    const double rk = 1.0 / k;
+    const double k2 = kx * kx + ky * ky;
+    const double rk = rsqrt(k2);                    // 1/k
+    const double k = k2 * rk;
+    if (!(h <= 0.0) && !(k > 0.0) && !isnan(k)) return RHS_ARGUMENT_OUT_OF_BOUNDS;
     const double kh = k * h;
-    const double m = -expm1(-2.0 * kh);  // 1 - exp(-2kh)
-    const double q = 1.0 - m;            // exp(-2kh)
-    const double r = 1.0 / (2.0 - m);
+    const double m = -expm1(-2.0 * kh);             // 1 - exp(-2kh)
+    const double q = 1.0 - m;                       // exp(-2kh)
+    const double inv_d = 1.0 / (m * (2.0 - m));     // one division for both below
+    const double r = m * inv_d;                     // 1 / (2 - m)
     const double th = m * r;                        // tanh(kh)
     const double kh_ch2 = 4.0 * kh * q * r * r;     // kh / cosh(kh)^2
-    const double inv_shch = 4.0 * q * r / m;        // 1 / (sinh(kh) cosh(kh))
+    const double inv_shch = 4.0 * q * (2.0 - m) * inv_d * r;  // 1 / (sinh cosh)
     const double gkt = kG * k * th;
     const double rs = rsqrt(gkt);                   // 1 / sqrt(g k tanh)
     double cg = (kG / 2.0) * (th + kh_ch2) * rs;
