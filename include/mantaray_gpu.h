@@ -180,6 +180,69 @@ int mr_ray_tracing_files(const char *bathymetry_path, const char *current_path,
                          double duration, double step_size, size_t rows_cap,
                          double *traj, int32_t *n_rows, uint8_t *status);
 
+/* ---- batched FP32 form ------------------------------------------------------
+ * ManyRays::trace_many (src/ray.rs:98-127) for millions of rays from many
+ * sources over several (bathymetry, current) scenarios, in single precision:
+ * the same ray equations, step and cell-gradient rule as the plain form, with
+ * FP32 right-hand side and interpolation, positions held as FP32 offsets from
+ * per-ray FP64 origins, and Kahan-compensated accumulation.  One persistent
+ * kernel; rays that end (grid exit, dry cell) are replaced from a device work
+ * queue.  Results: the state every `decimation` steps (f32) and the last
+ * valid state of each ray (f64).  All array arguments are device pointers.
+ * Calls on one mr_batch must not overlap on the GPU (they share its work
+ * queue). */
+typedef struct mr_batch mr_batch;
+typedef struct mr_batch_graph mr_batch_graph;
+
+/* Launch shape of the persistent kernel. */
+typedef struct mr_batch_config {
+  int block;           /* threads per block: a multiple of 32 in [32, 256] */
+  int blocks_per_sm;   /* resident blocks per SM of the persistent grid */
+  int rays_per_lane;   /* 1 or 2 rays interleaved per thread */
+  int rebase_interval; /* steps between FP64 origin rebases */
+} mr_batch_config;
+
+/* Per-ray status of the batched form. */
+#define MR_BATCH_COMPLETE 0       /* max_steps steps taken */
+#define MR_BATCH_OUT_OF_DOMAIN 1  /* a stage left the grid (reference: NaN stop) */
+#define MR_BATCH_DRY 2            /* depth <= 0 (reference: NaN group velocity) */
+#define MR_BATCH_BAD_WAVENUMBER 3 /* k <= 0 or non-finite */
+
+int mr_batch_default_config(mr_batch_config *cfg);
+
+/* Packs n_scenarios (bathymetry, current) pairs into FP32 cell records on
+ * the fields' device.  Bathymetry must be gridded with ascending, evenly
+ * spaced axes; the current gridded or constant. */
+int mr_batch_create(size_t n_scenarios, const mr_bathymetry *const *bathy,
+                    const mr_current *const *current, mr_batch **out);
+void mr_batch_destroy(mr_batch *b);
+
+/* Traces n rays from t0 with step dt for at most max_steps steps.
+ * ray_scenario [n] (null: all scenario 0); x0, y0, kx0, ky0 [n];
+ * saved [5][save_cap][n] f32 (t, x, y, kx, ky) every `decimation` steps, step
+ * 0 included (decimation 0: no rows; rows a ray does not reach are NaN);
+ * end_state [5][n] f64; n_steps, n_saved [n]; status [n]. */
+int mr_batch_trace_device(mr_batch *b, size_t n, const uint8_t *ray_scenario,
+                          const double *x0, const double *y0, const double *kx0,
+                          const double *ky0, double t0, double dt,
+                          int64_t max_steps, int64_t decimation, size_t save_cap,
+                          float *saved, double *end_state, int32_t *n_steps,
+                          int32_t *n_saved, uint8_t *status,
+                          const mr_batch_config *cfg, void *stream);
+
+/* The same call captured once in a CUDA graph over buffers sized for n_max
+ * rays (saved is [5][save_cap][n_max], end_state [5][n_max]); each launch
+ * replays it for the first n <= n_max rays of those buffers. */
+int mr_batch_graph_create(mr_batch *b, size_t n_max, const uint8_t *ray_scenario,
+                          const double *x0, const double *y0, const double *kx0,
+                          const double *ky0, double t0, double dt,
+                          int64_t max_steps, int64_t decimation, size_t save_cap,
+                          float *saved, double *end_state, int32_t *n_steps,
+                          int32_t *n_saved, uint8_t *status,
+                          const mr_batch_config *cfg, mr_batch_graph **out);
+int mr_batch_graph_launch(mr_batch_graph *g, size_t n, void *stream);
+void mr_batch_graph_destroy(mr_batch_graph *g);
+
 /* ---- NetCDF-3 access (host only, no GPU) ---------------------------------- */
 
 /* Reads variable `name` of a NetCDF-3 file converted to f64 (the reference's

@@ -34,7 +34,24 @@ SYMBOLS = (
     "mr_current_constant", "mr_current_destroy", "mr_num_steps", "mr_trace", "mr_trace_device",
     "mr_single_ray", "mr_single_ray_files", "mr_ray_tracing_files", "mr_netcdf3_read_f64",
     "mr_last_error", "mr_version", "mr_measure_fma_peak",
+    "mr_batch_default_config", "mr_batch_create", "mr_batch_destroy", "mr_batch_trace_device",
+    "mr_batch_graph_create", "mr_batch_graph_launch", "mr_batch_graph_destroy",
 )
+
+BATCH_COMPLETE = 0
+BATCH_OUT_OF_DOMAIN = 1
+BATCH_DRY = 2
+BATCH_BAD_WAVENUMBER = 3
+
+
+class BatchConfig(ctypes.Structure):
+    """mr_batch_config: launch shape of the persistent batched kernel."""
+
+    _fields_ = [("block", ctypes.c_int), ("blocks_per_sm", ctypes.c_int),
+                ("rays_per_lane", ctypes.c_int), ("rebase_interval", ctypes.c_int)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
 
 
 class MantarayError(RuntimeError):
@@ -92,6 +109,16 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "mr_last_error": (cs, []),
         "mr_version": (i32, []),
         "mr_measure_fma_peak": (i32, [i32, P(f64)]),
+        "mr_batch_default_config": (i32, [P(BatchConfig)]),
+        "mr_batch_create": (i32, [sz, P(vp), P(vp), pp]),
+        "mr_batch_destroy": (None, [vp]),
+        "mr_batch_trace_device": (i32, [vp, sz, vp, vp, vp, vp, vp, f64, f64, ctypes.c_int64,
+                                        ctypes.c_int64, sz, vp, vp, vp, vp, vp, P(BatchConfig), vp]),
+        "mr_batch_graph_create": (i32, [vp, sz, vp, vp, vp, vp, vp, f64, f64, ctypes.c_int64,
+                                        ctypes.c_int64, sz, vp, vp, vp, vp, vp, P(BatchConfig),
+                                        pp]),
+        "mr_batch_graph_launch": (i32, [vp, sz, vp]),
+        "mr_batch_graph_destroy": (None, [vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

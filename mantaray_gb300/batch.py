@@ -1,0 +1,227 @@
+"""Batched FP32 form: millions of rays over several scenarios in one
+persistent kernel, with CUDA-graph replay and a launch-shape autotuner.
+
+Python face of the mr_batch_* entry points of include/mantaray_gpu.h.  Device
+memory is torch CUDA tensors (plumbing only: the integration runs in the
+library's own kernels).
+"""
+
+from __future__ import annotations
+
+import ctypes
+import itertools
+import json
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _native as N
+from .fields import Bathymetry, Current
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+def default_config() -> N.BatchConfig:
+    cfg = N.BatchConfig()
+    N.check(N.load().mr_batch_default_config(ctypes.byref(cfg)))
+    return cfg
+
+
+def make_config(block=128, blocks_per_sm=4, rays_per_lane=1, rebase_interval=32) -> N.BatchConfig:
+    return N.BatchConfig(block, blocks_per_sm, rays_per_lane, rebase_interval)
+
+
+@dataclass
+class BatchResult:
+    """Outputs of one batched call (torch CUDA tensors)."""
+
+    saved: object       # [5][save_cap][n] f32 (t, x, y, kx, ky), NaN past each ray's rows
+    end_state: object   # [5][n] f64 last valid state
+    n_steps: object     # [n] int32
+    n_saved: object     # [n] int32
+    status: object      # [n] uint8 (MR_BATCH_*)
+
+
+class BatchTracer:
+    """Rays over a list of (bathymetry, current) scenarios in FP32."""
+
+    def __init__(self, scenarios):
+        L = N.load()
+        self._fields = list(scenarios)  # keep the field handles alive
+        n = len(self._fields)
+        bs = (ctypes.c_void_p * n)(*[b.handle.value for b, _ in self._fields])
+        cs = (ctypes.c_void_p * n)(*[c.handle.value for _, c in self._fields])
+        out = ctypes.c_void_p()
+        N.check(L.mr_batch_create(n, bs, cs, ctypes.byref(out)))
+        self._h = out
+        self.n_scenarios = n
+
+    def close(self):
+        if self._h and self._h.value:
+            N.load().mr_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass
+
+    @staticmethod
+    def alloc(n, max_steps, decimation, device="cuda"):
+        torch = _torch()
+        save_cap = (max_steps // decimation + 1) if decimation > 0 else 0
+        return BatchResult(
+            saved=torch.empty((5, save_cap, n), dtype=torch.float32, device=device)
+            if save_cap else torch.empty((5, 0, n), dtype=torch.float32, device=device),
+            end_state=torch.empty((5, n), dtype=torch.float64, device=device),
+            n_steps=torch.empty(n, dtype=torch.int32, device=device),
+            n_saved=torch.empty(n, dtype=torch.int32, device=device),
+            status=torch.empty(n, dtype=torch.uint8, device=device))
+
+    def trace(self, x0, y0, kx0, ky0, dt, max_steps, t0=0.0, decimation=0, scenario=None,
+              config=None, out: BatchResult | None = None, stream=None) -> BatchResult:
+        """Traces the rays (float64 CUDA tensors) asynchronously on `stream`."""
+        torch = _torch()
+        n = int(x0.numel())
+        cfg = config or default_config()
+        if out is None:
+            out = self.alloc(n, max_steps, decimation, device=x0.device)
+        if stream is None:
+            stream = torch.cuda.current_stream(x0.device)
+        sp = scenario.data_ptr() if scenario is not None else None
+        N.check(N.load().mr_batch_trace_device(
+            self._h, n, sp, x0.data_ptr(), y0.data_ptr(), kx0.data_ptr(), ky0.data_ptr(),
+            float(t0), float(dt), int(max_steps), int(decimation), int(out.saved.shape[1]),
+            out.saved.data_ptr() if out.saved.numel() else None, out.end_state.data_ptr(),
+            out.n_steps.data_ptr(), out.n_saved.data_ptr(), out.status.data_ptr(),
+            ctypes.byref(cfg), getattr(stream, "cuda_stream", stream)))
+        return out
+
+    def graph(self, x0, y0, kx0, ky0, dt, max_steps, t0=0.0, decimation=0, scenario=None,
+              config=None) -> "BatchGraph":
+        """Captures the call in a CUDA graph over buffers for x0.numel() rays."""
+        return BatchGraph(self, x0, y0, kx0, ky0, dt, max_steps, t0, decimation, scenario,
+                          config or default_config())
+
+    def autotune(self, x0, y0, kx0, ky0, dt, probe_steps, t0=0.0, scenario=None,
+                 candidates=None, repeats=2, cache_key=None) -> N.BatchConfig:
+        """Times every candidate launch shape on a probe run (the given rays
+        for `probe_steps` steps, endpoints only) and returns the fastest.
+        Results are cached in memory and in $MANTARAY_TUNE_CACHE (a JSON file)
+        when that is set."""
+        torch = _torch()
+        key = cache_key
+        cache_path = os.environ.get("MANTARAY_TUNE_CACHE")
+        if key and key in _TUNE_CACHE:
+            return make_config(**_TUNE_CACHE[key])
+        if key and cache_path and os.path.exists(cache_path):
+            stored = json.load(open(cache_path))
+            if key in stored:
+                _TUNE_CACHE[key] = stored[key]
+                return make_config(**stored[key])
+        if candidates is None:
+            candidates = [make_config(b, bps, rpl, 32)
+                          for b, bps, rpl in itertools.product((64, 128, 256), (2, 4, 8), (1, 2))
+                          if b * bps <= 2048]
+        out = self.alloc(int(x0.numel()), probe_steps, 0, device=x0.device)
+        best, best_t = None, float("inf")
+        stream = torch.cuda.current_stream(x0.device)
+        for cfg in candidates:
+            self.trace(x0, y0, kx0, ky0, dt, probe_steps, t0, 0, scenario, cfg, out, stream)
+            times = []
+            for _ in range(repeats):
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                self.trace(x0, y0, kx0, ky0, dt, probe_steps, t0, 0, scenario, cfg, out, stream)
+                e1.record(stream)
+                e1.synchronize()
+                times.append(e0.elapsed_time(e1))
+            t = min(times)
+            if t < best_t:
+                best, best_t = cfg, t
+        if key:
+            _TUNE_CACHE[key] = best.as_dict()
+            if cache_path:
+                stored = json.load(open(cache_path)) if os.path.exists(cache_path) else {}
+                stored[key] = best.as_dict()
+                json.dump(stored, open(cache_path, "w"), indent=1)
+        return best
+
+
+_TUNE_CACHE: dict = {}
+
+
+class BatchGraph:
+    """A batched call captured once and replayed for any n <= capacity."""
+
+    def __init__(self, tracer, x0, y0, kx0, ky0, dt, max_steps, t0, decimation, scenario, cfg):
+        self.tracer = tracer
+        self.n_max = int(x0.numel())
+        self.inputs = (x0, y0, kx0, ky0, scenario)  # kept alive: the graph reads them
+        self.out = tracer.alloc(self.n_max, max_steps, decimation, device=x0.device)
+        self.cfg = cfg
+        g = ctypes.c_void_p()
+        o = self.out
+        N.check(N.load().mr_batch_graph_create(
+            tracer._h, self.n_max, scenario.data_ptr() if scenario is not None else None,
+            x0.data_ptr(), y0.data_ptr(), kx0.data_ptr(), ky0.data_ptr(), float(t0), float(dt),
+            int(max_steps), int(decimation), int(o.saved.shape[1]),
+            o.saved.data_ptr() if o.saved.numel() else None, o.end_state.data_ptr(),
+            o.n_steps.data_ptr(), o.n_saved.data_ptr(), o.status.data_ptr(), ctypes.byref(cfg),
+            ctypes.byref(g)))
+        self._g = g
+
+    def launch(self, n=None, stream=None):
+        torch = _torch()
+        n = self.n_max if n is None else int(n)
+        if stream is None:
+            stream = torch.cuda.current_stream(self.inputs[0].device)
+        N.check(N.load().mr_batch_graph_launch(self._g, n, getattr(stream, "cuda_stream", stream)))
+
+    def close(self):
+        if self._g and self._g.value:
+            N.load().mr_batch_graph_destroy(self._g)
+            self._g = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass
+
+
+def endpoint_errors(end_state, n_steps, oracle_traj, oracle_rows):
+    """Endpoint error of batched results against full-precision trajectories
+    (traj[5][rows][n], e.g. the plain FP64 form's) at the batched form's last
+    valid step: relative position error |dx| / path length (path length along
+    the full-precision trajectory up to that step) and direction error
+    |d theta| (rad).  Rays that the batched form carried past the
+    full-precision trajectory's last finite row are counted, not compared."""
+    end = np.asarray(end_state)
+    steps = np.asarray(n_steps).astype(np.int64)
+    n = end.shape[1]
+    rows = np.asarray(oracle_rows).astype(np.int64)
+    traj = np.asarray(oracle_traj)
+    idx = np.arange(n)
+    last_ok = np.all(np.isfinite(traj[1:, rows - 1, idx]), axis=0)
+    last_finite = np.where(last_ok, rows - 1, rows - 2)
+    cmp = steps <= last_finite
+    row = np.where(cmp, steps, 0)
+    ox, oy = traj[1, row, idx], traj[2, row, idx]
+    okx, oky = traj[3, row, idx], traj[4, row, idx]
+    dxy = np.hypot(end[1] - ox, end[2] - oy)
+    seg = np.hypot(np.diff(traj[1], axis=0), np.diff(traj[2], axis=0))
+    seg = np.where(np.arange(seg.shape[0])[:, None] < row[None, :], seg, 0.0)
+    path = np.nansum(seg, axis=0)
+    rel = np.where(path > 0, dxy / np.maximum(path, 1e-300), 0.0)
+    dth = np.abs(np.angle(np.exp(1j * (np.arctan2(end[4], end[3]) - np.arctan2(oky, okx)))))
+    return {"rel_position": rel[cmp], "direction": dth[cmp], "compared": int(np.sum(cmp)),
+            "past_end": int(np.sum(~cmp)), "early_stop": int(np.sum(steps < last_finite)),
+            "n": n}

@@ -30,6 +30,8 @@ UNITS = {
     "api.cu": [],
     "netcdf3.cpp": [],
     "diag.cu": [],
+    "rk4_f32.cu": [],
+    "batch_api.cu": [],
 }
 
 

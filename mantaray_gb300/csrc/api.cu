@@ -16,24 +16,11 @@
 
 #include "../../include/mantaray_gpu.h"
 #include "fields.h"
+#include "handles.h"
 #include "kernels.h"
 #include "netcdf3.h"
 
-struct mr_bathymetry {
-  mr::BathyDev dev{};
-  int device = 0;
-  bool one_point_axis = false;  // the reference panics on its first lookup
-  std::vector<void *> mem;      // device allocations owned by the handle
-};
-
-struct mr_current {
-  mr::CurrentDev dev{};
-  int device = 0;
-  bool one_point_axis = false;
-  std::vector<void *> mem;
-};
-
-namespace {
+namespace mr {
 
 thread_local std::string g_last_error;
 
@@ -52,30 +39,13 @@ int cuda_fail(cudaError_t e, const char *what) {
               what, cudaGetErrorString(e), cudaGetErrorName(e));
 }
 
-#define MR_CUDA(call)                                   \
-  do {                                                  \
-    cudaError_t e_ = (call);                            \
-    if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
-  } while (0)
+}  // namespace mr
 
-// Makes `device` current for the lifetime of the guard.
-class DeviceGuard {
- public:
-  explicit DeviceGuard(int device) {
-    ok_ = cudaGetDevice(&prev_) == cudaSuccess;
-    if (ok_ && prev_ != device) ok_ = cudaSetDevice(device) == cudaSuccess;
-    switched_ = ok_ && prev_ != device;
-  }
-  ~DeviceGuard() {
-    if (switched_) cudaSetDevice(prev_);
-  }
-  bool ok() const { return ok_; }
+using mr::cuda_fail;
+using mr::DeviceGuard;
+using mr::fail;
 
- private:
-  int prev_ = 0;
-  bool ok_ = false;
-  bool switched_ = false;
-};
+namespace {
 
 // Device copy of a host array, owned (and freed) by the handle.
 template <typename T>
@@ -314,7 +284,7 @@ int launch(const mr_bathymetry *b, const mr_current *c, size_t n, const double *
 
 extern "C" {
 
-const char *mr_last_error(void) { return g_last_error.c_str(); }
+const char *mr_last_error(void) { return mr::g_last_error.c_str(); }
 
 int mr_version(void) { return 100; }
 

@@ -1,0 +1,65 @@
+// batch.h -- device structures of the batched FP32 form.
+//
+// A scenario is one (bathymetry, current) pair.  For the FP32 form each field
+// is repacked once, on the device, into cells: one cell per grid square,
+// indexed by its south-west corner (i, j), holding everything a lookup
+// inside that square needs, so a lookup is a few 16-byte loads from one
+// contiguous record:
+//   bathymetry cell (8 floats, 32 B):  h(i,j) h(i+1,j) h(i,j+1) h(i+1,j+1)
+//                                      dh/dx dh/dy 0 0
+//   current cell (12 floats, 48 B):    u x4, v x4 (same corner order),
+//                                      du/dx du/dy dv/dx dv/dy
+// The gradients are the reference's cell forward differences
+// (src/bathymetry/cartesian_netcdf3.rs:119-134,
+// src/current/cartesian_current.rs:515-536), so the FP32 form integrates the
+// same equations as the plain form, in single precision.
+#pragma once
+
+#include <stdint.h>
+
+namespace mr {
+
+struct PackedGrid {
+  const float4 *cells;   // [(ny-1)*(nx-1)] records of `vec4` float4s
+  int nx, ny;            // grid points
+  double x0, y0;         // first axis values
+  double sp_x, sp_y;     // axis spacing (a[1] - a[0])
+  float inv_sp_x, inv_sp_y;
+  int kind;              // 0 grid, 1 constant (current only)
+  float cu, cv;          // constant current
+};
+
+struct ScenarioDev {
+  PackedGrid bathy;      // 2 float4 per cell
+  PackedGrid current;    // 3 float4 per cell
+};
+
+// Per-ray termination status of the batched form.
+enum BatchStatus : uint8_t {
+  BATCH_COMPLETE = 0,      // all max_steps steps taken
+  BATCH_OUT_OF_DOMAIN = 1, // a stage left the bathymetry or current grid
+  BATCH_DRY = 2,           // depth <= 0
+  BATCH_BAD_WAVENUMBER = 3,// k <= 0 or non-finite state
+};
+
+struct BatchArgs {
+  const ScenarioDev *scen;   // [n_scenarios]
+  int n_scenarios;
+  const uint8_t *ray_scenario;  // [n] scenario per ray, or null (all scenario 0)
+  int64_t n;                 // rays of this call
+  const double *x0, *y0, *kx0, *ky0;  // [n] initial states
+  double t0, dt;
+  int64_t max_steps;
+  int64_t decimation;        // store every `decimation`-th step (0: endpoints only)
+  int64_t save_cap;          // rows of `saved` per ray
+  int64_t n_stride;          // ray stride of `saved` (>= n; the buffer's capacity)
+  int rebase_interval;       // steps between FP64 origin rebases
+  float *saved;              // [5][save_cap][n_stride] f32 t, x, y, kx, ky
+  double *end_state;         // [5][n_stride] f64 t, x, y, kx, ky of the last valid state
+  int32_t *n_steps;          // [n] steps taken
+  int32_t *n_saved;          // [n] rows stored in `saved`
+  uint8_t *status;           // [n] BatchStatus
+  unsigned long long *queue; // work-queue head (scratch, zeroed before the launch)
+};
+
+}  // namespace mr

@@ -1,0 +1,320 @@
+// batch_api.cu -- C ABI of the batched FP32 form (include/mantaray_gpu.h):
+// scenario packing, device-buffer tracing, and CUDA-graph replay.
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <string.h>
+
+#include <vector>
+
+#include "../../include/mantaray_gpu.h"
+#include "batch.h"
+#include "handles.h"
+#include "kernels.h"
+
+struct mr_batch {
+  int device = 0;
+  int n_scenarios = 0;
+  std::vector<mr::ScenarioDev> host_scen;
+  mr::ScenarioDev *scen = nullptr;   // device copy of host_scen
+  std::vector<void *> mem;           // packed cells
+  unsigned long long *queue = nullptr;  // work-queue head (device scratch)
+};
+
+struct mr_batch_graph {
+  mr_batch *batch = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaGraphNode_t kernel_node = nullptr;
+  cudaKernelNodeParams params{};
+  mr::BatchArgs args{};
+  size_t n_max = 0;
+};
+
+namespace {
+
+using mr::cuda_fail;
+using mr::DeviceGuard;
+using mr::fail;
+
+int pack_bathy(mr_batch *b, const mr_bathymetry *h, mr::PackedGrid *g, cudaStream_t s) {
+  if (h->dev.kind != mr::BATHY_GRID)
+    return fail(MR_ERR_INVALID_ARGUMENT, "the batched form needs gridded bathymetry");
+  if (h->one_point_axis)
+    return fail(MR_ERR_INVALID_ARGUMENT, "a bathymetry axis has a single point");
+  if (!(h->dev.xspace > 0.0) || !(h->dev.yspace > 0.0))
+    return fail(MR_ERR_INVALID_ARGUMENT, "the batched form needs ascending, evenly spaced axes");
+  const size_t ncell = (h->dev.nx - 1) * (h->dev.ny - 1);
+  void *cells = nullptr;
+  MR_CUDA(cudaMalloc(&cells, ncell * 2 * sizeof(float4)));
+  b->mem.push_back(cells);
+  MR_CUDA(mr::launch_pack_bathy(h->dev, static_cast<float4 *>(cells), s));
+  g->cells = static_cast<const float4 *>(cells);
+  g->nx = static_cast<int>(h->dev.nx);
+  g->ny = static_cast<int>(h->dev.ny);
+  g->x0 = static_cast<double>(h->dev.x0);
+  g->y0 = static_cast<double>(h->dev.y0);
+  g->sp_x = h->dev.xspace;
+  g->sp_y = h->dev.yspace;
+  g->inv_sp_x = static_cast<float>(1.0 / h->dev.xspace);
+  g->inv_sp_y = static_cast<float>(1.0 / h->dev.yspace);
+  g->kind = 0;
+  return MR_OK;
+}
+
+int pack_current(mr_batch *b, const mr_current *c, mr::PackedGrid *g, cudaStream_t s) {
+  if (c->dev.kind == mr::CURRENT_CONSTANT) {
+    g->kind = 1;
+    g->cu = static_cast<float>(c->dev.cu);
+    g->cv = static_cast<float>(c->dev.cv);
+    g->cells = nullptr;
+    g->nx = g->ny = 2;
+    g->x0 = g->y0 = 0.0;
+    g->sp_x = g->sp_y = 1.0;
+    g->inv_sp_x = g->inv_sp_y = 1.0f;
+    return MR_OK;
+  }
+  if (c->one_point_axis) return fail(MR_ERR_INVALID_ARGUMENT, "a current axis has a single point");
+  if (!(c->dev.xspace > 0.0) || !(c->dev.yspace > 0.0))
+    return fail(MR_ERR_INVALID_ARGUMENT, "the batched form needs ascending, evenly spaced axes");
+  const size_t ncell = (c->dev.nx - 1) * (c->dev.ny - 1);
+  void *cells = nullptr;
+  MR_CUDA(cudaMalloc(&cells, ncell * 3 * sizeof(float4)));
+  b->mem.push_back(cells);
+  MR_CUDA(mr::launch_pack_current(c->dev, static_cast<float4 *>(cells), s));
+  g->cells = static_cast<const float4 *>(cells);
+  g->nx = static_cast<int>(c->dev.nx);
+  g->ny = static_cast<int>(c->dev.ny);
+  g->x0 = c->dev.x0;
+  g->y0 = c->dev.y0;
+  g->sp_x = c->dev.xspace;
+  g->sp_y = c->dev.yspace;
+  g->inv_sp_x = static_cast<float>(1.0 / c->dev.xspace);
+  g->inv_sp_y = static_cast<float>(1.0 / c->dev.yspace);
+  g->kind = 0;
+  return MR_OK;
+}
+
+int check_config(const mr_batch_config *cfg) {
+  if (!cfg) return fail(MR_ERR_INVALID_ARGUMENT, "null config");
+  if (cfg->block < 32 || cfg->block > 256 || cfg->block % 32)
+    return fail(MR_ERR_INVALID_ARGUMENT, "block must be a multiple of 32 in [32, 256]");
+  if (cfg->blocks_per_sm < 1 || cfg->blocks_per_sm > 32)
+    return fail(MR_ERR_INVALID_ARGUMENT, "blocks_per_sm must be in [1, 32]");
+  if (cfg->rays_per_lane != 1 && cfg->rays_per_lane != 2)
+    return fail(MR_ERR_INVALID_ARGUMENT, "rays_per_lane must be 1 or 2");
+  if (cfg->rebase_interval < 1)
+    return fail(MR_ERR_INVALID_ARGUMENT, "rebase_interval must be >= 1");
+  return MR_OK;
+}
+
+int fill_args(mr_batch *b, size_t n, size_t n_stride, const uint8_t *ray_scenario,
+              const double *x0, const double *y0, const double *kx0, const double *ky0, double t0,
+              double dt, int64_t max_steps, int64_t decimation, size_t save_cap, float *saved,
+              double *end_state, int32_t *n_steps, int32_t *n_saved, uint8_t *status,
+              const mr_batch_config *cfg, mr::BatchArgs *a) {
+  if (!b) return fail(MR_ERR_INVALID_ARGUMENT, "null batch");
+  int rc = check_config(cfg);
+  if (rc) return rc;
+  if (n > n_stride) return fail(MR_ERR_INVALID_ARGUMENT, "n exceeds the buffers' capacity");
+  if (n_stride > 0 && (!x0 || !y0 || !kx0 || !ky0 || !end_state || !n_steps || !n_saved || !status))
+    return fail(MR_ERR_INVALID_ARGUMENT, "null array argument");
+  if (decimation < 0 || max_steps < 0 || max_steps >= INT32_MAX)
+    return fail(MR_ERR_INVALID_ARGUMENT, "bad max_steps or decimation");
+  if (decimation > 0) {
+    if (!saved) return fail(MR_ERR_INVALID_ARGUMENT, "null saved buffer with decimation > 0");
+    if (static_cast<int64_t>(save_cap) < max_steps / decimation + 1)
+      return fail(MR_ERR_CAPACITY, "save_cap %zu < max_steps / decimation + 1 = %lld", save_cap,
+                  static_cast<long long>(max_steps / decimation + 1));
+  }
+  if (!(dt > 0.0) || !isfinite(t0)) return fail(MR_ERR_INVALID_ARGUMENT, "dt must be > 0");
+  a->scen = b->scen;
+  a->n_scenarios = b->n_scenarios;
+  a->ray_scenario = ray_scenario;
+  a->n = static_cast<int64_t>(n);
+  a->x0 = x0; a->y0 = y0; a->kx0 = kx0; a->ky0 = ky0;
+  a->t0 = t0;
+  a->dt = dt;
+  a->max_steps = max_steps;
+  a->decimation = decimation;
+  a->save_cap = static_cast<int64_t>(save_cap);
+  a->n_stride = static_cast<int64_t>(n_stride);
+  a->rebase_interval = cfg->rebase_interval;
+  a->saved = saved;
+  a->end_state = end_state;
+  a->n_steps = n_steps;
+  a->n_saved = n_saved;
+  a->status = status;
+  a->queue = b->queue;
+  return MR_OK;
+}
+
+// Stream work of one batched call: reset the queue, NaN-fill the saved rows
+// (rows a ray does not reach stay NaN, as the reference pads them), launch.
+cudaError_t enqueue(const mr::BatchArgs &a, const mr_batch_config *cfg, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(a.queue, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return e;
+  if (a.decimation > 0 && a.save_cap > 0) {
+    e = cudaMemsetAsync(a.saved, 0xFF, sizeof(float) * 5 * a.save_cap * a.n_stride, s);
+    if (e != cudaSuccess) return e;
+  }
+  return mr::launch_rk4_f32(a, cfg->block, cfg->blocks_per_sm, cfg->rays_per_lane, s);
+}
+
+}  // namespace
+
+extern "C" {
+
+int mr_batch_default_config(mr_batch_config *cfg) {
+  if (!cfg) return fail(MR_ERR_INVALID_ARGUMENT, "null config");
+  cfg->block = 128;
+  cfg->blocks_per_sm = 4;
+  cfg->rays_per_lane = 1;
+  cfg->rebase_interval = 32;
+  return MR_OK;
+}
+
+int mr_batch_create(size_t n_scenarios, const mr_bathymetry *const *bathy,
+                    const mr_current *const *current, mr_batch **out) {
+  if (!out) return fail(MR_ERR_INVALID_ARGUMENT, "null output handle pointer");
+  *out = nullptr;
+  if (n_scenarios == 0 || n_scenarios > 256 || !bathy || !current)
+    return fail(MR_ERR_INVALID_ARGUMENT, "1 to 256 scenarios are needed");
+  for (size_t i = 0; i < n_scenarios; ++i) {
+    if (!bathy[i] || !current[i]) return fail(MR_ERR_INVALID_ARGUMENT, "null field handle");
+    if (bathy[i]->device != bathy[0]->device || current[i]->device != bathy[0]->device)
+      return fail(MR_ERR_INVALID_ARGUMENT, "fields live on different devices");
+  }
+  DeviceGuard g(bathy[0]->device);
+  if (!g.ok()) return fail(MR_ERR_CUDA, "cannot select the fields' device");
+  mr_batch *b = new mr_batch();
+  b->device = bathy[0]->device;
+  b->n_scenarios = static_cast<int>(n_scenarios);
+  b->host_scen.resize(n_scenarios);
+  cudaStream_t s = cudaStreamPerThread;
+  int rc = MR_OK;
+  for (size_t i = 0; i < n_scenarios && rc == MR_OK; ++i) {
+    rc = pack_bathy(b, bathy[i], &b->host_scen[i].bathy, s);
+    if (rc == MR_OK) rc = pack_current(b, current[i], &b->host_scen[i].current, s);
+  }
+  cudaError_t e = cudaSuccess;
+  if (rc == MR_OK) e = cudaMalloc(reinterpret_cast<void **>(&b->scen), n_scenarios * sizeof(mr::ScenarioDev));
+  if (rc == MR_OK && e == cudaSuccess)
+    e = cudaMemcpyAsync(b->scen, b->host_scen.data(), n_scenarios * sizeof(mr::ScenarioDev),
+                        cudaMemcpyHostToDevice, s);
+  if (rc == MR_OK && e == cudaSuccess)
+    e = cudaMalloc(reinterpret_cast<void **>(&b->queue), sizeof(unsigned long long));
+  if (rc == MR_OK && e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (rc == MR_OK && e != cudaSuccess) rc = cuda_fail(e, "building the batched scenarios");
+  if (rc != MR_OK) {
+    mr_batch_destroy(b);
+    return rc;
+  }
+  *out = b;
+  return MR_OK;
+}
+
+void mr_batch_destroy(mr_batch *b) {
+  if (!b) return;
+  DeviceGuard g(b->device);
+  for (void *p : b->mem) cudaFree(p);
+  if (b->scen) cudaFree(b->scen);
+  if (b->queue) cudaFree(b->queue);
+  delete b;
+}
+
+int mr_batch_trace_device(mr_batch *b, size_t n, const uint8_t *ray_scenario, const double *x0,
+                          const double *y0, const double *kx0, const double *ky0, double t0,
+                          double dt, int64_t max_steps, int64_t decimation, size_t save_cap,
+                          float *saved, double *end_state, int32_t *n_steps, int32_t *n_saved,
+                          uint8_t *status, const mr_batch_config *cfg, void *stream) {
+  mr::BatchArgs a{};
+  int rc = fill_args(b, n, n, ray_scenario, x0, y0, kx0, ky0, t0, dt, max_steps, decimation,
+                     save_cap, saved, end_state, n_steps, n_saved, status, cfg, &a);
+  if (rc) return rc;
+  if (n == 0) return MR_OK;
+  DeviceGuard g(b->device);
+  if (!g.ok()) return fail(MR_ERR_CUDA, "cannot select the batch's device");
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : cudaStreamPerThread;
+  cudaError_t e = enqueue(a, cfg, s);
+  if (e != cudaSuccess) return cuda_fail(e, "rk4_f32 launch");
+  return MR_OK;
+}
+
+int mr_batch_graph_create(mr_batch *b, size_t n_max, const uint8_t *ray_scenario,
+                          const double *x0, const double *y0, const double *kx0,
+                          const double *ky0, double t0, double dt, int64_t max_steps,
+                          int64_t decimation, size_t save_cap, float *saved, double *end_state,
+                          int32_t *n_steps, int32_t *n_saved, uint8_t *status,
+                          const mr_batch_config *cfg, mr_batch_graph **out) {
+  if (!out) return fail(MR_ERR_INVALID_ARGUMENT, "null output handle pointer");
+  *out = nullptr;
+  mr::BatchArgs a{};
+  int rc = fill_args(b, n_max, n_max, ray_scenario, x0, y0, kx0, ky0, t0, dt, max_steps,
+                     decimation, save_cap, saved, end_state, n_steps, n_saved, status, cfg, &a);
+  if (rc) return rc;
+  DeviceGuard g(b->device);
+  if (!g.ok()) return fail(MR_ERR_CUDA, "cannot select the batch's device");
+  mr_batch_graph *gr = new mr_batch_graph();
+  gr->batch = b;
+  gr->args = a;
+  gr->n_max = n_max;
+  cudaStream_t s = nullptr;
+  cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    cudaError_t le = enqueue(a, cfg, s);
+    e = cudaStreamEndCapture(s, &gr->graph);
+    if (le != cudaSuccess) e = le;
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&gr->exec, gr->graph, 0);
+  size_t count = 0;
+  if (e == cudaSuccess) e = cudaGraphGetNodes(gr->graph, nullptr, &count);
+  std::vector<cudaGraphNode_t> nodes(count);
+  if (e == cudaSuccess && count) e = cudaGraphGetNodes(gr->graph, nodes.data(), &count);
+  for (size_t i = 0; e == cudaSuccess && i < count; ++i) {
+    cudaGraphNodeType type;
+    e = cudaGraphNodeGetType(nodes[i], &type);
+    if (e == cudaSuccess && type == cudaGraphNodeTypeKernel) {
+      gr->kernel_node = nodes[i];
+      e = cudaGraphKernelNodeGetParams(nodes[i], &gr->params);
+    }
+  }
+  if (s) cudaStreamDestroy(s);
+  if (e == cudaSuccess && !gr->kernel_node) e = cudaErrorInvalidValue;
+  if (e != cudaSuccess) {
+    mr_batch_graph_destroy(gr);
+    return cuda_fail(e, "capturing the batched graph");
+  }
+  *out = gr;
+  return MR_OK;
+}
+
+int mr_batch_graph_launch(mr_batch_graph *gr, size_t n, void *stream) {
+  if (!gr) return fail(MR_ERR_INVALID_ARGUMENT, "null graph");
+  if (n > gr->n_max) return fail(MR_ERR_CAPACITY, "n %zu exceeds the graph's capacity %zu", n, gr->n_max);
+  DeviceGuard g(gr->batch->device);
+  if (!g.ok()) return fail(MR_ERR_CUDA, "cannot select the batch's device");
+  // n is a kernel argument: the executable graph's kernel node takes the new
+  // value for this and later launches (launches already queued keep theirs).
+  gr->args.n = static_cast<int64_t>(n);
+  void *kargs[1] = {&gr->args};
+  cudaKernelNodeParams p = gr->params;
+  p.kernelParams = kargs;
+  p.extra = nullptr;
+  cudaError_t e = cudaGraphExecKernelNodeSetParams(gr->exec, gr->kernel_node, &p);
+  if (e == cudaSuccess)
+    e = cudaGraphLaunch(gr->exec, stream ? static_cast<cudaStream_t>(stream) : cudaStreamPerThread);
+  if (e != cudaSuccess) return cuda_fail(e, "launching the batched graph");
+  return MR_OK;
+}
+
+void mr_batch_graph_destroy(mr_batch_graph *gr) {
+  if (!gr) return;
+  DeviceGuard g(gr->batch ? gr->batch->device : 0);
+  if (gr->exec) cudaGraphExecDestroy(gr->exec);
+  if (gr->graph) cudaGraphDestroy(gr->graph);
+  delete gr;
+}
+
+}  // extern "C"

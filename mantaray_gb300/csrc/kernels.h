@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "batch.h"
 #include "fields.h"
 
 namespace mr {
@@ -25,5 +26,12 @@ struct TraceArgs {
 
 cudaError_t launch_rk4_f64(const BathyDev &b, const CurrentDev &c, const TraceArgs &a,
                            int stop_rule, int identity_math, cudaStream_t stream);
+
+// Batched FP32 form: cell packing of one field (one thread per cell) and the
+// persistent integrator (grid = SMs x blocks_per_sm).
+cudaError_t launch_pack_bathy(const BathyDev &b, float4 *cells, cudaStream_t stream);
+cudaError_t launch_pack_current(const CurrentDev &c, float4 *cells, cudaStream_t stream);
+cudaError_t launch_rk4_f32(const BatchArgs &a, int block, int blocks_per_sm, int rays_per_lane,
+                           cudaStream_t stream);
 
 }  // namespace mr

@@ -1,0 +1,358 @@
+// rk4_f32.cu -- K2, the batched FP32 ray integrator, and K5, its grid prep.
+//
+// K5 (pack_*_cells): repacks a bathymetry / current grid of the plain form
+// (f64 values in HBM) into the cell records of batch.h, one thread per cell.
+//
+// K2 (rk4_f32_kernel): a persistent kernel, grid = SMs x resident blocks.
+// Each lane holds RAYS_PER_LANE rays.  A lane whose ray has ended refills from
+// a device work queue: the warp ballots its empty slots, one lane reserves
+// that many ray indices with a single atomicAdd and the indices are handed out
+// by rank within the ballot, so lanes never idle while work remains and rays
+// of very different lifetimes (domain exits, dry cells) keep every lane busy.
+// There is no waiting on other blocks or threads anywhere in the kernel.
+//
+// Precision: the right-hand side and the interpolation run in FP32 (the
+// identity form of the RHS, see ray_exact.cuh, in single precision).  Each
+// ray's position is an FP32 offset from an FP64 origin; offsets and
+// wavenumbers are accumulated with Kahan compensation, and every
+// `rebase_interval` steps the offset is folded into the FP64 origin, which
+// keeps the offsets (and their rounding) small over tens of thousands of
+// steps.  FP64 is used only for that rebase and for the stored positions.
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "batch.h"
+#include "fields.h"
+#include "kernels.h"
+
+namespace mr {
+
+namespace {
+
+// ---------------------------------------------------------------- K5 prep --
+
+__global__ void pack_bathy_cells(BathyDev b, float4 *cells) {
+  const int64_t ncx = static_cast<int64_t>(b.nx) - 1, ncy = static_cast<int64_t>(b.ny) - 1;
+  const int64_t c = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (c >= ncx * ncy) return;
+  const int64_t i = c % ncx, j = c / ncx;
+  const uint64_t sw = b.nx * j + i, se = sw + 1, nw = sw + b.nx, ne = nw + 1;
+  float4 r0, r1;
+  if (ne < b.depth_len) {
+    const double d00 = b.depth[sw], d10 = b.depth[se], d01 = b.depth[nw], d11 = b.depth[ne];
+    r0 = make_float4(__double2float_rn(d00), __double2float_rn(d10), __double2float_rn(d01),
+                     __double2float_rn(d11));
+    r1 = make_float4(__double2float_rn((d10 - d00) / b.xspace),
+                     __double2float_rn((d01 - d00) / b.yspace), 0.0f, 0.0f);
+  } else {  // corners past the end of the depth array: no water
+    const float nan = __int_as_float(0x7fffffff);
+    r0 = make_float4(nan, nan, nan, nan);
+    r1 = make_float4(nan, nan, 0.0f, 0.0f);
+  }
+  cells[2 * c] = r0;
+  cells[2 * c + 1] = r1;
+}
+
+__global__ void pack_current_cells(CurrentDev cu, float4 *cells) {
+  const int64_t ncx = static_cast<int64_t>(cu.nx) - 1, ncy = static_cast<int64_t>(cu.ny) - 1;
+  const int64_t c = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (c >= ncx * ncy) return;
+  const int64_t i = c % ncx, j = c / ncx;
+  const uint64_t sw = cu.nx * j + i, se = sw + 1, nw = sw + cu.nx, ne = nw + 1;
+  float4 r0, r1, r2;
+  if (ne < cu.u_len && ne < cu.v_len) {
+    const double u00 = cu.u[sw], u10 = cu.u[se], u01 = cu.u[nw], u11 = cu.u[ne];
+    const double v00 = cu.v[sw], v10 = cu.v[se], v01 = cu.v[nw], v11 = cu.v[ne];
+    r0 = make_float4(__double2float_rn(u00), __double2float_rn(u10), __double2float_rn(u01),
+                     __double2float_rn(u11));
+    r1 = make_float4(__double2float_rn(v00), __double2float_rn(v10), __double2float_rn(v01),
+                     __double2float_rn(v11));
+    r2 = make_float4(__double2float_rn((u10 - u00) / cu.xspace),
+                     __double2float_rn((u01 - u00) / cu.yspace),
+                     __double2float_rn((v10 - v00) / cu.xspace),
+                     __double2float_rn((v01 - v00) / cu.yspace));
+  } else {
+    const float nan = __int_as_float(0x7fffffff);
+    r0 = r1 = r2 = make_float4(nan, nan, nan, nan);
+  }
+  cells[3 * c] = r0;
+  cells[3 * c + 1] = r1;
+  cells[3 * c + 2] = r2;
+}
+
+// ------------------------------------------------------------------ K2 --
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr float kGf = 9.8f;
+
+// Position of a lane on one grid: integer cell base of its origin plus the
+// origin's fractional cell offset.
+struct GridPos {
+  int i0, j0;
+  float f0, g0;
+};
+
+__device__ __forceinline__ GridPos grid_pos(const PackedGrid &g, double ox, double oy) {
+  GridPos p;
+  const double ux = (ox - g.x0) / g.sp_x, uy = (oy - g.y0) / g.sp_y;
+  const double fx = floor(ux), fy = floor(uy);
+  // clamp far-away origins so the int conversion stays defined; such a lane
+  // fails the in-range test of its first lookup
+  p.i0 = static_cast<int>(fmin(fmax(fx, -1.0e9), 1.0e9));
+  p.j0 = static_cast<int>(fmin(fmax(fy, -1.0e9), 1.0e9));
+  p.f0 = static_cast<float>(ux - fx);
+  p.g0 = static_cast<float>(uy - fy);
+  if (!(ux == ux) || !(uy == uy)) { p.i0 = -2000000000; p.f0 = 0.0f; }
+  return p;
+}
+
+// Cell index and in-cell fractions at offset (px, py) from the origin; false
+// when outside the grid's cells.
+__device__ __forceinline__ bool locate(const PackedGrid &g, const GridPos &p, float px, float py,
+                                       int64_t *cell, float *fx, float *fy) {
+  const float ux = p.f0 + px * g.inv_sp_x;
+  const float uy = p.g0 + py * g.inv_sp_y;
+  const float flx = floorf(ux), fly = floorf(uy);
+  const float cx = static_cast<float>(p.i0) + flx, cy = static_cast<float>(p.j0) + fly;
+  if (!(cx >= 0.0f && cx <= static_cast<float>(g.nx - 2) && cy >= 0.0f &&
+        cy <= static_cast<float>(g.ny - 2)))
+    return false;
+  *cell = static_cast<int64_t>(p.j0 + static_cast<int>(fly)) * (g.nx - 1) +
+          (p.i0 + static_cast<int>(flx));
+  *fx = ux - flx;
+  *fy = uy - fly;
+  return true;
+}
+
+__device__ __forceinline__ float bilin(const float4 &v, float fx, float fy) {
+  // v = (v(i,j), v(i+1,j), v(i,j+1), v(i+1,j+1))
+  const float a = fmaf(fx, v.y - v.x, v.x);
+  const float b = fmaf(fx, v.w - v.z, v.z);
+  return fmaf(fy, b - a, a);
+}
+
+struct RayLane {
+  int64_t ray;      // -1: empty slot, -2: no work left
+  int scen;
+  double ox, oy;    // FP64 origin
+  GridPos pb, pc;   // origin on the bathymetry and current grids
+  float px, py, kx, ky;      // offsets and wavenumber
+  float cpx, cpy, ckx, cky;  // Kahan compensations
+  int64_t step;
+  int32_t saved;
+};
+
+// Right-hand side in FP32 at offset (px, py); returns a BatchStatus.
+__device__ __forceinline__ int rhs_f32(const ScenarioDev &s, const RayLane &L, float px, float py,
+                                       float kx, float ky, float d[4]) {
+  int64_t cb;
+  float fx, fy;
+  if (!locate(s.bathy, L.pb, px, py, &cb, &fx, &fy)) return BATCH_OUT_OF_DOMAIN;
+  const float4 b0 = __ldg(s.bathy.cells + 2 * cb);
+  const float4 b1 = __ldg(s.bathy.cells + 2 * cb + 1);
+  const float h = bilin(b0, fx, fy);
+  float u, v, dudx = 0.0f, dudy = 0.0f, dvdx = 0.0f, dvdy = 0.0f;
+  if (s.current.kind == 0) {
+    int64_t cc;
+    float gx, gy;
+    if (!locate(s.current, L.pc, px, py, &cc, &gx, &gy)) return BATCH_OUT_OF_DOMAIN;
+    const float4 c0 = __ldg(s.current.cells + 3 * cc);
+    const float4 c1 = __ldg(s.current.cells + 3 * cc + 1);
+    const float4 c2 = __ldg(s.current.cells + 3 * cc + 2);
+    u = bilin(c0, gx, gy);
+    v = bilin(c1, gx, gy);
+    dudx = c2.x; dudy = c2.y; dvdx = c2.z; dvdy = c2.w;
+  } else {
+    u = s.current.cu;
+    v = s.current.cv;
+  }
+  if (!(h > 0.0f)) return h <= 0.0f ? BATCH_DRY : BATCH_OUT_OF_DOMAIN;
+  const float k2 = kx * kx + ky * ky;
+  if (!(k2 > 0.0f) || !(k2 < 3.0e38f)) return BATCH_BAD_WAVENUMBER;
+  const float rk = rsqrtf(k2);
+  const float k = k2 * rk;
+  const float kh = k * h;
+  const float m = -expm1f(-2.0f * kh);  // 1 - exp(-2kh)
+  const float q = 1.0f - m;
+  const float inv_d = 1.0f / (m * (2.0f - m));
+  const float r = m * inv_d;            // 1 / (2 - m)
+  const float th = m * r;               // tanh(kh)
+  const float kh_ch2 = 4.0f * kh * q * r * r;
+  const float inv_shch = 4.0f * q * (2.0f - m) * inv_d * r;
+  const float gkt = kGf * k * th;
+  const float rs = rsqrtf(gkt);
+  const float cg = 0.5f * kGf * (th + kh_ch2) * rs;
+  const float f = -0.5f * k * inv_shch * (gkt * rs);
+  d[0] = fmaf(cg, kx * rk, u);
+  d[1] = fmaf(cg, ky * rk, v);
+  d[2] = f * b1.x - kx * dudx - ky * dvdx;
+  d[3] = f * b1.y - kx * dudy - ky * dvdy;
+  return BATCH_COMPLETE;
+}
+
+__device__ __forceinline__ void kahan_add(float &sum, float &comp, float inc) {
+  const float y = inc - comp;
+  const float t = sum + y;
+  comp = (t - sum) - y;
+  sum = t;
+}
+
+__device__ __forceinline__ void rebase(const ScenarioDev &s, RayLane &L) {
+  L.ox += static_cast<double>(L.px) - static_cast<double>(L.cpx);
+  L.oy += static_cast<double>(L.py) - static_cast<double>(L.cpy);
+  L.px = L.py = L.cpx = L.cpy = 0.0f;
+  L.pb = grid_pos(s.bathy, L.ox, L.oy);
+  L.pc = grid_pos(s.current, L.ox, L.oy);
+}
+
+__device__ __forceinline__ void save_row(const BatchArgs &a, const RayLane &L) {
+  if (L.saved >= a.save_cap) return;
+  const int64_t plane = a.save_cap * a.n_stride;
+  float *p = a.saved + static_cast<int64_t>(L.saved) * a.n_stride + L.ray;
+  p[0] = static_cast<float>(a.t0 + static_cast<double>(L.step) * a.dt);
+  p[plane] = static_cast<float>(L.ox + (static_cast<double>(L.px) - static_cast<double>(L.cpx)));
+  p[2 * plane] = static_cast<float>(L.oy + (static_cast<double>(L.py) - static_cast<double>(L.cpy)));
+  p[3 * plane] = L.kx - L.ckx;
+  p[4 * plane] = L.ky - L.cky;
+}
+
+__device__ __forceinline__ void finish(const BatchArgs &a, RayLane &L, int status) {
+  const int64_t r = L.ray;
+  a.end_state[r] = a.t0 + static_cast<double>(L.step) * a.dt;
+  a.end_state[a.n_stride + r] = L.ox + (static_cast<double>(L.px) - static_cast<double>(L.cpx));
+  a.end_state[2 * a.n_stride + r] = L.oy + (static_cast<double>(L.py) - static_cast<double>(L.cpy));
+  a.end_state[3 * a.n_stride + r] = static_cast<double>(L.kx) - static_cast<double>(L.ckx);
+  a.end_state[4 * a.n_stride + r] = static_cast<double>(L.ky) - static_cast<double>(L.cky);
+  a.n_steps[r] = static_cast<int32_t>(L.step);
+  a.n_saved[r] = L.saved;
+  a.status[r] = static_cast<uint8_t>(status);
+  L.ray = -1;
+}
+
+__device__ __forceinline__ void start(const BatchArgs &a, RayLane &L, int64_t r) {
+  L.ray = r;
+  L.scen = a.ray_scenario ? static_cast<int>(a.ray_scenario[r]) : 0;
+  if (L.scen >= a.n_scenarios) L.scen = 0;
+  const ScenarioDev &s = a.scen[L.scen];
+  L.ox = a.x0[r];
+  L.oy = a.y0[r];
+  L.px = L.py = L.cpx = L.cpy = L.ckx = L.cky = 0.0f;
+  L.kx = static_cast<float>(a.kx0[r]);
+  L.ky = static_cast<float>(a.ky0[r]);
+  L.pb = grid_pos(s.bathy, L.ox, L.oy);
+  L.pc = grid_pos(s.current, L.ox, L.oy);
+  L.step = 0;
+  L.saved = 0;
+  if (a.decimation > 0) {
+    save_row(a, L);
+    L.saved = 1;
+  }
+}
+
+// One RK4 step of lane L.  Returns BATCH_COMPLETE while the ray goes on.
+__device__ __forceinline__ int advance(const BatchArgs &a, RayLane &L) {
+  const ScenarioDev &s = a.scen[L.scen];
+  const float dt = static_cast<float>(a.dt);
+  const float half = 0.5f * dt;
+  float k1[4], k2[4], k3[4], k4[4];
+  int st = rhs_f32(s, L, L.px, L.py, L.kx, L.ky, k1);
+  if (st == BATCH_COMPLETE)
+    st = rhs_f32(s, L, fmaf(half, k1[0], L.px), fmaf(half, k1[1], L.py),
+                 fmaf(half, k1[2], L.kx), fmaf(half, k1[3], L.ky), k2);
+  if (st == BATCH_COMPLETE)
+    st = rhs_f32(s, L, fmaf(half, k2[0], L.px), fmaf(half, k2[1], L.py),
+                 fmaf(half, k2[2], L.kx), fmaf(half, k2[3], L.ky), k3);
+  if (st == BATCH_COMPLETE)
+    st = rhs_f32(s, L, fmaf(dt, k3[0], L.px), fmaf(dt, k3[1], L.py), fmaf(dt, k3[2], L.kx),
+                 fmaf(dt, k3[3], L.ky), k4);
+  if (st != BATCH_COMPLETE) return st;
+  const float sixth = dt * (1.0f / 6.0f);
+  kahan_add(L.px, L.cpx, sixth * (k1[0] + 2.0f * (k2[0] + k3[0]) + k4[0]));
+  kahan_add(L.py, L.cpy, sixth * (k1[1] + 2.0f * (k2[1] + k3[1]) + k4[1]));
+  kahan_add(L.kx, L.ckx, sixth * (k1[2] + 2.0f * (k2[2] + k3[2]) + k4[2]));
+  kahan_add(L.ky, L.cky, sixth * (k1[3] + 2.0f * (k2[3] + k3[3]) + k4[3]));
+  ++L.step;
+  if (a.decimation > 0 && L.step % a.decimation == 0) {
+    save_row(a, L);
+    ++L.saved;
+  }
+  if (L.step % a.rebase_interval == 0) rebase(s, L);
+  return BATCH_COMPLETE;
+}
+
+template <int RPT>
+__global__ void __launch_bounds__(256) rk4_f32_kernel(BatchArgs a) {
+  const int lane = threadIdx.x & 31;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  const int64_t n = a.n;
+  RayLane L[RPT];
+#pragma unroll
+  for (int j = 0; j < RPT; ++j) L[j].ray = -1;
+  while (true) {
+    // refill empty slots from the work queue, one atomic per warp and slot
+#pragma unroll
+    for (int j = 0; j < RPT; ++j) {
+      const unsigned need = __ballot_sync(kFull, L[j].ray == -1);
+      if (need) {
+        const int leader = __ffs(need) - 1;
+        unsigned long long base = 0;
+        if (lane == leader) base = atomicAdd(a.queue, static_cast<unsigned long long>(__popc(need)));
+        base = __shfl_sync(kFull, base, leader);
+        if (L[j].ray == -1) {
+          const int64_t r = static_cast<int64_t>(base) + __popc(need & lt_mask);
+          if (r < n) start(a, L[j], r);
+          else L[j].ray = -2;
+        }
+      }
+    }
+    bool live = false;
+#pragma unroll
+    for (int j = 0; j < RPT; ++j) live |= L[j].ray >= 0;
+    if (!__any_sync(kFull, live)) break;
+#pragma unroll
+    for (int j = 0; j < RPT; ++j) {
+      if (L[j].ray < 0) continue;
+      if (L[j].step >= a.max_steps) {
+        finish(a, L[j], BATCH_COMPLETE);
+        continue;
+      }
+      const int st = advance(a, L[j]);
+      if (st != BATCH_COMPLETE) finish(a, L[j], st);
+    }
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_pack_bathy(const BathyDev &b, float4 *cells, cudaStream_t stream) {
+  const int64_t ncell = static_cast<int64_t>(b.nx - 1) * static_cast<int64_t>(b.ny - 1);
+  if (ncell <= 0) return cudaSuccess;
+  pack_bathy_cells<<<static_cast<unsigned>((ncell + 255) / 256), 256, 0, stream>>>(b, cells);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pack_current(const CurrentDev &c, float4 *cells, cudaStream_t stream) {
+  const int64_t ncell = static_cast<int64_t>(c.nx - 1) * static_cast<int64_t>(c.ny - 1);
+  if (ncell <= 0) return cudaSuccess;
+  pack_current_cells<<<static_cast<unsigned>((ncell + 255) / 256), 256, 0, stream>>>(c, cells);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rk4_f32(const BatchArgs &a, int block, int blocks_per_sm, int rays_per_lane,
+                           cudaStream_t stream) {
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  const unsigned grid = static_cast<unsigned>(sms * blocks_per_sm);
+  if (rays_per_lane == 2)
+    rk4_f32_kernel<2><<<grid, block, 0, stream>>>(a);
+  else
+    rk4_f32_kernel<1><<<grid, block, 0, stream>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace mr
