@@ -23,14 +23,16 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC]
 
-# Translation units and their extra flags.  The exact-arithmetic kernels are
-# compiled with -fmad=false: the reference (Rust) never contracts a*b+c.
+# Translation units and their extra flags.  The integrators are compiled with
+# -fmad=false: the plain kernel because the reference (Rust) never contracts
+# a*b+c, the batched kernel so that its explicit fmaf calls are its only
+# fused operations (same bits for every launch shape).
 UNITS = {
     "rk4_f64.cu": ["-fmad=false"],
     "api.cu": [],
     "netcdf3.cpp": [],
     "diag.cu": [],
-    "rk4_f32.cu": [],
+    "rk4_f32.cu": ["-fmad=false"],
     "batch_api.cu": [],
 }
 

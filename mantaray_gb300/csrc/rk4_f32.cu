@@ -18,6 +18,10 @@
 // `rebase_interval` steps the offset is folded into the FP64 origin, which
 // keeps the offsets (and their rounding) small over tens of thousands of
 // steps.  FP64 is used only for that rebase and for the stored positions.
+//
+// Compiled with -fmad=false and every fused multiply-add written as fmaf, so
+// each ray's arithmetic is fixed by the source: results are bit-identical for
+// every launch shape (block size, blocks per SM, rays per lane).
 
 #include <cuda_runtime.h>
 #include <math.h>
@@ -112,8 +116,8 @@ __device__ __forceinline__ GridPos grid_pos(const PackedGrid &g, double ox, doub
 // when outside the grid's cells.
 __device__ __forceinline__ bool locate(const PackedGrid &g, const GridPos &p, float px, float py,
                                        int64_t *cell, float *fx, float *fy) {
-  const float ux = p.f0 + px * g.inv_sp_x;
-  const float uy = p.g0 + py * g.inv_sp_y;
+  const float ux = fmaf(px, g.inv_sp_x, p.f0);
+  const float uy = fmaf(py, g.inv_sp_y, p.g0);
   const float flx = floorf(ux), fly = floorf(uy);
   const float cx = static_cast<float>(p.i0) + flx, cy = static_cast<float>(p.j0) + fly;
   if (!(cx >= 0.0f && cx <= static_cast<float>(g.nx - 2) && cy >= 0.0f &&
@@ -169,7 +173,7 @@ __device__ __forceinline__ int rhs_f32(const ScenarioDev &s, const RayLane &L, f
     v = s.current.cv;
   }
   if (!(h > 0.0f)) return h <= 0.0f ? BATCH_DRY : BATCH_OUT_OF_DOMAIN;
-  const float k2 = kx * kx + ky * ky;
+  const float k2 = fmaf(kx, kx, ky * ky);
   if (!(k2 > 0.0f) || !(k2 < 3.0e38f)) return BATCH_BAD_WAVENUMBER;
   const float rk = rsqrtf(k2);
   const float k = k2 * rk;
@@ -187,8 +191,8 @@ __device__ __forceinline__ int rhs_f32(const ScenarioDev &s, const RayLane &L, f
   const float f = -0.5f * k * inv_shch * (gkt * rs);
   d[0] = fmaf(cg, kx * rk, u);
   d[1] = fmaf(cg, ky * rk, v);
-  d[2] = f * b1.x - kx * dudx - ky * dvdx;
-  d[3] = f * b1.y - kx * dudy - ky * dvdy;
+  d[2] = fmaf(-ky, dvdx, fmaf(-kx, dudx, f * b1.x));
+  d[3] = fmaf(-ky, dvdy, fmaf(-kx, dudy, f * b1.y));
   return BATCH_COMPLETE;
 }
 
@@ -269,10 +273,12 @@ __device__ __forceinline__ int advance(const BatchArgs &a, RayLane &L) {
                  fmaf(dt, k3[3], L.ky), k4);
   if (st != BATCH_COMPLETE) return st;
   const float sixth = dt * (1.0f / 6.0f);
-  kahan_add(L.px, L.cpx, sixth * (k1[0] + 2.0f * (k2[0] + k3[0]) + k4[0]));
-  kahan_add(L.py, L.cpy, sixth * (k1[1] + 2.0f * (k2[1] + k3[1]) + k4[1]));
-  kahan_add(L.kx, L.ckx, sixth * (k1[2] + 2.0f * (k2[2] + k3[2]) + k4[2]));
-  kahan_add(L.ky, L.cky, sixth * (k1[3] + 2.0f * (k2[3] + k3[3]) + k4[3]));
+#pragma unroll
+  for (int q = 0; q < 4; ++q) k1[q] = sixth * fmaf(2.0f, k2[q] + k3[q], k1[q] + k4[q]);
+  kahan_add(L.px, L.cpx, k1[0]);
+  kahan_add(L.py, L.cpy, k1[1]);
+  kahan_add(L.kx, L.ckx, k1[2]);
+  kahan_add(L.ky, L.cky, k1[3]);
   ++L.step;
   if (a.decimation > 0 && L.step % a.decimation == 0) {
     save_row(a, L);
