@@ -87,3 +87,150 @@ def seamount(n_rays: int = 65536, steps: int = 4000, seed: int = 1001) -> Worklo
     return Workload(f"seamount_{n_rays}rays_2001x2001_dt1_{steps}steps", x.astype(np.float32),
                     x.astype(np.float32), depth, x, x, u, v, x0, y0, kx0, ky0, 0.0, float(steps),
                     1.0, {"grid": (n, n), "spacing": 50.0})
+
+
+def shelf_bump(n_rays: int = 262144, steps: int = 3000, bump_scale: float = 1.0,
+               seed: int = 1002) -> Workload:
+    """Differentiation case: 262,144 rays on a 512 x 512 grid at 200 m.
+    Bathymetry: a linear shelf from 3,000 m (x = 0) to 20 m (far edge) with a
+    1,500 m Gaussian shoal (sigma 8 km) at (30 km, 51.2 km), floored at 5 m;
+    `bump_scale` multiplies the shoal (1.1 gives the loss targets).  Current:
+    a Gaussian jet u(y) = 1.0 exp(-(y - 51.2 km)^2 / (2 (5 km)^2)), v = 0.
+    Rays from x = 0, y ~ U[10, 92] km, directions ~ U(+-30 deg), T ~ U[8, 14] s;
+    dt = 1 s for 3,000 steps."""
+    rng = np.random.default_rng(seed)
+    n = 512
+    x = np.arange(n, dtype=np.float64) * 200.0
+    L = x[-1]
+    shelf = 3000.0 - 2980.0 * (x / L)
+    r2 = (x[None, :] - 30000.0) ** 2 + (x[:, None] - 51200.0) ** 2
+    depth = np.maximum(5.0, shelf[None, :] - bump_scale * 1500.0 * np.exp(-r2 / (2.0 * 8000.0 ** 2)))
+    u = np.broadcast_to(np.exp(-((x[:, None] - 51200.0) ** 2) / (2.0 * 5000.0 ** 2)), (n, n)).copy()
+    v = np.zeros((n, n))
+    y0 = rng.uniform(10000.0, 92000.0, n_rays)
+    theta = rng.uniform(-np.deg2rad(30.0), np.deg2rad(30.0), n_rays)
+    period = rng.uniform(8.0, 14.0, n_rays)
+    x0 = np.zeros(n_rays)
+    kx0, ky0 = wavenumber_vector(period, np.full(n_rays, 3000.0), theta)
+    return Workload(f"shelf_bump_{n_rays}rays_512x512_dt1_{steps}steps", x.astype(np.float32),
+                    x.astype(np.float32), depth, x, x, u, v, x0, y0, kx0, ky0, 0.0, float(steps),
+                    1.0, {"grid": (n, n), "spacing": 200.0, "bump_scale": bump_scale})
+
+
+def _gaussian_vortices(rng, x, y, count, speed_lo, speed_hi, sigma_lo, sigma_hi):
+    """u = d(psi)/dy, v = -d(psi)/dx of a streamfunction made of `count`
+    Gaussian vortices psi_j = A_j exp(-r^2 / (2 s_j^2)); each vortex's peak
+    speed (at r = s_j) is drawn from [speed_lo, speed_hi] with a random sign.
+    Each vortex is evaluated within 6 sigma of its centre (beyond that its
+    velocity is below 1e-7 of its peak)."""
+    u = np.zeros((y.size, x.size))
+    v = np.zeros((y.size, x.size))
+    dxg, dyg = x[1] - x[0], y[1] - y[0]
+    for _ in range(count):
+        cx, cy = rng.uniform(x[0], x[-1]), rng.uniform(y[0], y[-1])
+        s = rng.uniform(sigma_lo, sigma_hi)
+        a = rng.choice([-1.0, 1.0]) * rng.uniform(speed_lo, speed_hi) * s * np.exp(0.5)
+        i0 = max(0, int((cx - 6 * s - x[0]) / dxg)); i1 = min(x.size, int((cx + 6 * s - x[0]) / dxg) + 2)
+        j0 = max(0, int((cy - 6 * s - y[0]) / dyg)); j1 = min(y.size, int((cy + 6 * s - y[0]) / dyg) + 2)
+        dx = x[None, i0:i1] - cx
+        dy = y[j0:j1, None] - cy
+        g = a * np.exp(-(dx * dx + dy * dy) / (2.0 * s * s)) / (s * s)
+        u[j0:j1, i0:i1] += -dy * g
+        v[j0:j1, i0:i1] += dx * g
+    return u, v
+
+
+def multi_source(n_sources: int = 1024, rays_per_source: int = 4096, n_scenarios: int = 8,
+                 n: int = 2048, steps: int = 20000, seed: int = 1003):
+    """Batching + precision case: 8 scenarios of 2,048 x 2,048 grids at 100 m.
+    Each scenario's bathymetry is 4,000 m minus 32 seeded Gaussian shoals
+    (amplitude 500-4,500 m, sigma 5-40 km) clipped to 20-4,000 m; its current
+    comes from a streamfunction of 16 Gaussian vortices with peak speeds
+    0.2-1.5 m/s (sigma 5-25 km).  1,024 point sources (128 per scenario, away
+    from the edges) emit 4,096 rays each, directions ~ U[0, 2 pi), periods
+    ~ U[6, 18] s.  dt = 2 s, up to 20,000 steps.  Returns (scenarios, rays):
+    scenarios = [(bx, by, depth, cx, cy, u, v)], rays = dict of arrays with a
+    `scenario` column; rays are grouped by scenario."""
+    rng = np.random.default_rng(seed)
+    x = np.arange(n, dtype=np.float64) * 100.0
+    scenarios = []
+    depth_fns = []
+    for _ in range(n_scenarios):
+        bumps = [(rng.uniform(x[0], x[-1]), rng.uniform(x[0], x[-1]), rng.uniform(500, 4500),
+                  rng.uniform(5000, 40000)) for _ in range(32)]
+        X, Y = x[None, :], x[:, None]
+        h = np.full((n, n), 4000.0)
+        for cx, cy, a, s in bumps:
+            h -= a * np.exp(-((X - cx) ** 2 + (Y - cy) ** 2) / (2.0 * s * s))
+        h = np.clip(h, 20.0, 4000.0)
+        u, v = _gaussian_vortices(rng, x, x, 16, 0.2, 1.5, 5000.0, 25000.0)
+        scenarios.append((x.astype(np.float32), x.astype(np.float32), h, x, x, u, v))
+
+        def depth_at(px, py, bumps=bumps):
+            hh = np.full(px.shape, 4000.0)
+            for cx, cy, a, s in bumps:
+                hh -= a * np.exp(-((px - cx) ** 2 + (py - cy) ** 2) / (2.0 * s * s))
+            return np.clip(hh, 20.0, 4000.0)
+
+        depth_fns.append(depth_at)
+    per_scen = n_sources // n_scenarios
+    xs, ys, kxs, kys, sid = [], [], [], [], []
+    margin = 10000.0
+    for s in range(n_scenarios):
+        sx = rng.uniform(margin, x[-1] - margin, per_scen)
+        sy = rng.uniform(margin, x[-1] - margin, per_scen)
+        px = np.repeat(sx, rays_per_source)
+        py = np.repeat(sy, rays_per_source)
+        theta = rng.uniform(0.0, 2.0 * np.pi, px.size)
+        period = rng.uniform(6.0, 18.0, px.size)
+        kx, ky = wavenumber_vector(period, depth_fns[s](px, py), theta)
+        xs.append(px); ys.append(py); kxs.append(kx); kys.append(ky)
+        sid.append(np.full(px.size, s, np.uint8))
+    rays = {"x0": np.concatenate(xs), "y0": np.concatenate(ys), "kx0": np.concatenate(kxs),
+            "ky0": np.concatenate(kys), "scenario": np.concatenate(sid), "t0": 0.0, "dt": 2.0,
+            "steps": steps}
+    return scenarios, rays
+
+
+def shelf_slope(n: int = 8192, n_rays: int = 16777216, steps: int = 50000, seed: int = 1004):
+    """Large single-scenario case: 8,192 x 8,192 grid at 50 m.  Bathymetry: a
+    continental shelf-slope profile along x (4,000 m deep at the entry edge,
+    a tanh slope centred at 300 km, 15 km wide, up to a 60 m shelf) plus
+    seeded 2-D random-phase roughness with a k^-3 spectrum scaled to 50 m rms,
+    floored at 5 m.  Current: a meandering jet along x (1 m/s, 20 km wide,
+    meander amplitude 30 km, wavelength 150 km) plus 64 seeded Gaussian eddies
+    (0.2-1.0 m/s, sigma 5-20 km).  Swell enters at x = 0 with y ~ U over the
+    edge, directions ~ U(+-15 deg), periods ~ U[10, 16] s; dt = 2 s, up to
+    50,000 steps.  Returns (fields, rays) like multi_source (one scenario)."""
+    rng = np.random.default_rng(seed)
+    x = np.arange(n, dtype=np.float64) * 50.0
+    profile = 60.0 + (4000.0 - 60.0) * 0.5 * (1.0 - np.tanh((x - 300000.0) / 15000.0))
+    # random-phase k^-3 roughness (FFT synthesis on the grid)
+    kx = np.fft.fftfreq(n, d=50.0)
+    ky = np.fft.rfftfreq(n, d=50.0)
+    kk = np.hypot(kx[:, None], ky[None, :])
+    amp = np.zeros_like(kk)
+    nz = kk > 0
+    amp[nz] = kk[nz] ** -1.5  # |F|^2 ~ k^-3
+    phase = np.exp(2j * np.pi * rng.random(kk.shape))
+    rough = np.fft.irfft2(amp * phase, s=(n, n))
+    rough *= 50.0 / np.sqrt(np.mean(rough * rough))
+    depth = np.maximum(5.0, profile[None, :] + rough)
+    del rough, amp, phase, kk
+    Y = x[:, None]
+    yc = x[-1] / 2 + 30000.0 * np.sin(2.0 * np.pi * x[None, :] / 150000.0)
+    u = 1.0 * np.exp(-((Y - yc) ** 2) / (2.0 * 20000.0 ** 2))
+    v = np.zeros_like(u)
+    eu, ev = _gaussian_vortices(rng, x, x, 64, 0.2, 1.0, 5000.0, 20000.0)
+    u += eu
+    v += ev
+    del eu, ev
+    y0 = rng.uniform(0.0, x[-1], n_rays)
+    theta = rng.uniform(-np.deg2rad(15.0), np.deg2rad(15.0), n_rays)
+    period = rng.uniform(10.0, 16.0, n_rays)
+    x0 = np.zeros(n_rays)
+    kx0, ky0 = wavenumber_vector(period, np.full(n_rays, profile[0]), theta)
+    fields = (x.astype(np.float32), x.astype(np.float32), depth, x, x, u, v)
+    rays = {"x0": x0, "y0": y0, "kx0": kx0, "ky0": ky0, "scenario": None, "t0": 0.0, "dt": 2.0,
+            "steps": steps}
+    return fields, rays
