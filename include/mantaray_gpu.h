@@ -243,6 +243,26 @@ int mr_batch_graph_create(mr_batch *b, size_t n_max, const uint8_t *ray_scenario
 int mr_batch_graph_launch(mr_batch_graph *g, size_t n, void *stream);
 void mr_batch_graph_destroy(mr_batch_graph *g);
 
+/* mr_batch_trace_device without any device allocation.  No counterpart in
+ * the reference.  For callers that cannot call cudaMalloc when they trace
+ * (device memory owned by another runtime's pool, or a loop that must not
+ * allocate): the kernel's scratch -- its work-queue head and this call's copy
+ * of the scenario table -- lives in a static 16 KiB device array that every
+ * GPU loading the library keeps until exit, instead of in memory the library
+ * allocates.  Limit: at most MR_BATCH_STATIC_MAX_SCENARIOS scenarios
+ * (MR_ERR_CAPACITY beyond).  The first call on a device looks up the array's
+ * device address; make that first call before any stream capture.  All calls
+ * share the array: calls that overlap on the GPU race, so serialise them.
+ * Arguments and results as mr_batch_trace_device. */
+#define MR_BATCH_STATIC_MAX_SCENARIOS 64
+int mr_batch_trace_device_static(mr_batch *b, size_t n, const uint8_t *ray_scenario,
+                                 const double *x0, const double *y0, const double *kx0,
+                                 const double *ky0, double t0, double dt,
+                                 int64_t max_steps, int64_t decimation, size_t save_cap,
+                                 float *saved, double *end_state, int32_t *n_steps,
+                                 int32_t *n_saved, uint8_t *status,
+                                 const mr_batch_config *cfg, void *stream);
+
 /* ---- NetCDF-3 access (host only, no GPU) ---------------------------------- */
 
 /* Reads variable `name` of a NetCDF-3 file converted to f64 (the reference's

@@ -36,7 +36,10 @@ SYMBOLS = (
     "mr_last_error", "mr_version", "mr_measure_fma_peak",
     "mr_batch_default_config", "mr_batch_create", "mr_batch_destroy", "mr_batch_trace_device",
     "mr_batch_graph_create", "mr_batch_graph_launch", "mr_batch_graph_destroy",
+    "mr_batch_trace_device_static",
 )
+
+BATCH_STATIC_MAX_SCENARIOS = 64
 
 BATCH_COMPLETE = 0
 BATCH_OUT_OF_DOMAIN = 1
@@ -118,6 +121,9 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
                                         ctypes.c_int64, sz, vp, vp, vp, vp, vp, P(BatchConfig),
                                         pp]),
         "mr_batch_graph_launch": (i32, [vp, sz, vp]),
+        "mr_batch_trace_device_static": (i32, [vp, sz, vp, vp, vp, vp, vp, f64, f64,
+                                               ctypes.c_int64, ctypes.c_int64, sz, vp, vp, vp,
+                                               vp, vp, P(BatchConfig), vp]),
         "mr_batch_graph_destroy": (None, [vp]),
     }
     for name, (res, args) in sig.items():

@@ -34,6 +34,7 @@ UNITS = {
     "diag.cu": [],
     "rk4_f32.cu": ["-fmad=false"],
     "batch_api.cu": [],
+    "batch_static.cu": [],
 }
 
 

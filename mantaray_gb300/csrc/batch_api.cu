@@ -9,17 +9,10 @@
 
 #include "../../include/mantaray_gpu.h"
 #include "batch.h"
+#include "batch_handle.h"
 #include "handles.h"
 #include "kernels.h"
 
-struct mr_batch {
-  int device = 0;
-  int n_scenarios = 0;
-  std::vector<mr::ScenarioDev> host_scen;
-  mr::ScenarioDev *scen = nullptr;   // device copy of host_scen
-  std::vector<void *> mem;           // packed cells
-  unsigned long long *queue = nullptr;  // work-queue head (device scratch)
-};
 
 struct mr_batch_graph {
   mr_batch *batch = nullptr;
