@@ -39,11 +39,16 @@ L2_FLUSH_BYTES = 512 << 20  # > 129 MB L2
 # stored 40 B output row (t, x, y, kx, ky).
 GRID_BYTES_PER_RAY_STEP = 4 * 3 * 4 * 8
 OUT_BYTES_PER_ROW = 5 * 8
+# FP32 floating-point operations one ray-step of the batched kernel executes
+# (FADD/FMUL = 1, FFMA = 2), counted by ncu on the seamount workload.
+FP32_FLOP_PER_RAY_STEP = 541.7
 # FP64 floating-point operations one ray-step executes (DADD/DMUL = 1,
 # DFMA = 2), per right-hand-side arithmetic, counted by ncu on the plain
 # kernel over the seamount workload
 # (sm__sass_thread_inst_executed_op_d{add,mul,fma}_pred_on; profiles/).
-FP64_FLOP_PER_RAY_STEP = {"libm": None, "identity": None}
+FP64_FLOP_PER_RAY_STEP = {"libm": 1840.0, "identity": 384.0}
+# FP64-pipe instructions per ray-step (sm__inst_executed_pipe_fp64 x 32, same captures)
+FP64_PIPE_INST_PER_RAY_STEP = {"libm": 1317.0, "identity": 448.0}
 
 
 def parse():
@@ -60,6 +65,15 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--math", default="identity", choices=["identity", "libm"],
                    help="right-hand-side arithmetic of the plain FP64 kernel")
+    p.add_argument("--form", default="plain", choices=["plain", "batched"],
+                   help="plain FP64 drop-in (default) or the batched FP32 form")
+    p.add_argument("--workload", default="seamount",
+                   choices=["seamount", "shelf_slope", "multi_source"],
+                   help="batched form only: the seamount case, the 8192^2 shelf-slope case "
+                        "(graph-replayed calls with varied ray counts) or the 8-scenario "
+                        "multi-source case")
+    p.add_argument("--grid", type=int, default=None, help="grid points per axis override")
+    p.add_argument("--no-autotune", action="store_true")
     return p.parse_args()
 
 
@@ -330,7 +344,10 @@ def gb300_arm(args, rank: int, world: int, local_rank: int):
         roofline = {"bound": "fp64", "achieved": fp64_achieved, "peak": fp64_peak.value,
                     "unit": "TFLOP/s", "frac": fp64_achieved / fp64_peak.value,
                     "peak_source": "measured: FP64 FMA-chain kernel on this GPU, this run",
-                    "flop_per_ray_step": flop_per_rs}
+                    "flop_per_ray_step": flop_per_rs,
+                    "pipe_issue_frac": rs_per_s_kernel * FP64_PIPE_INST_PER_RAY_STEP[args.math]
+                    / (fp64_peak.value * 1e12 / 2.0),
+                    "pipe_issue_note": "FP64-pipe instructions/s over the FMA-chain DFMA/s"}
     else:
         roofline = {"bound": "fp64", "achieved": None, "peak": fp64_peak.value,
                     "unit": "TFLOP/s", "frac": None,
@@ -339,7 +356,10 @@ def gb300_arm(args, rank: int, world: int, local_rank: int):
                        "frac": hbm_achieved / hbm_peak,
                        "bytes_per_ray_step": GRID_BYTES_PER_RAY_STEP + OUT_BYTES_PER_ROW,
                        "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"}
-    roofline["traffic"] = None
+    # DRAM bytes of one full launch, scaled from the ncu capture of 16,384 rays
+    # x 400 steps (221.9 MB) by ray-steps (profiles/rk4_f64_seamount_16384rays_400steps.md)
+    roofline["traffic"] = 221.9e6 * ray_steps / (16384 * 400)
+    roofline["traffic_note"] = "scaled from a 16,384-ray x 400-step ncu capture by ray-steps"
     roofline["kernel_ms"] = 1e3 * kernel_s
 
     cpu = None
@@ -366,6 +386,246 @@ def gb300_arm(args, rank: int, world: int, local_rank: int):
         dist.destroy_process_group()
 
 
+def batched_arm(args, rank: int, world: int, local_rank: int):
+    """The batched FP32 form (rk4_f32) on one of the benchmark workloads, with
+    the plain FP64 form timed beside it on a subset of the same rays and the
+    endpoint error of the FP32 results against it."""
+    import ctypes
+
+    import torch
+
+    import mantaray_gb300 as mr
+    from mantaray_gb300 import workloads as W
+    from mantaray_gb300.batch import BatchTracer, default_config, endpoint_errors
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist  # noqa: F811
+
+        dist.init_process_group("nccl", device_id=dev)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    graph_mode = False
+    decimation = 0
+    if args.workload == "seamount":
+        w = W.seamount(n_rays=args.rays, steps=args.trace_steps)
+        fields = [(w.bx, w.by, w.depth, w.cx, w.cy, w.u, w.v)]
+        rays = {"x0": w.x0, "y0": w.y0, "kx0": w.kx0, "ky0": w.ky0, "scenario": None,
+                "t0": w.t0, "dt": w.dt, "steps": mr.num_steps(w.t0, w.t_end, w.dt)}
+        name = w.name
+    elif args.workload == "multi_source":
+        n = args.grid or 2048
+        fields, rays = W.multi_source(n=n, steps=args.trace_steps if args.trace_steps != 4000
+                                      else 20000)
+        decimation = 100
+        name = f"multi_source_{rays['x0'].size}rays_8x{n}x{n}_dt2_{rays['steps']}steps_every100"
+    else:
+        n = args.grid or 8192
+        steps = args.trace_steps if args.trace_steps != 4000 else 2000
+        fields, rays = W.shelf_slope(n=n, n_rays=args.rays if args.rays != 65536 else 16777216,
+                                     steps=steps)
+        fields = [fields]
+        graph_mode = True
+        name = (f"shelf_slope_{rays['x0'].size}rays_{n}x{n}_dt2_{steps}steps_graph_replay_"
+                f"n_varied_50pct")
+    handles = [(mr.Bathymetry.grid(f[0], f[1], f[2]), mr.Current.grid(f[3], f[4], f[5], f[6]))
+               for f in fields]
+    tracer = BatchTracer(handles)
+    n_all = rays["x0"].size
+    ins = [torch.from_numpy(np.ascontiguousarray(rays[k])).to(dev) for k in ("x0", "y0", "kx0", "ky0")]
+    sid = (torch.from_numpy(rays["scenario"]).to(dev) if rays["scenario"] is not None else None)
+    steps, dt, t0 = rays["steps"], rays["dt"], rays["t0"]
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    cfg = default_config()
+    tuned = None
+    if not args.no_autotune:
+        probe = min(n_all, 1 << 20)
+        pin = [t[:probe] for t in ins]
+        cfg = tracer.autotune(*pin, dt, min(steps, 200), t0=t0,
+                              scenario=sid[:probe] if sid is not None else None,
+                              cache_key=f"{torch.cuda.get_device_name(dev)}:{name}:{probe}")
+        tuned = cfg.as_dict()
+
+    rng = np.random.default_rng(7)
+    if graph_mode:
+        # capacity 1.5x the nominal count; each call traces U[0.5, 1.5] x nominal rays
+        nominal = n_all * 2 // 3
+        g = tracer.graph(*ins, dt, steps, t0=t0, decimation=decimation, scenario=sid, config=cfg)
+        counts = rng.integers(nominal // 2, n_all + 1, args.warmup + args.steps)
+        out = g.out
+
+        def one(i):
+            g.launch(int(counts[i]), stream=stream)
+            return int(counts[i])
+    else:
+        out = tracer.alloc(n_all, steps, decimation, device=dev)
+
+        def one(i):
+            tracer.trace(*ins, dt, steps, t0=t0, decimation=decimation, scenario=sid, config=cfg,
+                         out=out, stream=stream)
+            return n_all
+
+    for i in range(args.warmup):
+        one(i)
+    torch.cuda.synchronize()
+    times, done_steps, launches = [], 0, 0
+    with ClockSampler(local_rank) as clocks:
+        barrier()
+        torch.cuda.synchronize()
+        for i in range(args.steps):
+            flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            nrays = one(args.warmup + i)
+            e1.record(stream)
+            launches += 1
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+            done_steps += int(out.n_steps[:nrays].to(torch.int64).sum().item())
+        torch.cuda.synchronize()
+        barrier()
+    clock = clocks.summary()
+    local_t = sum(times)
+    t_max = local_t
+    if dist is not None:
+        tt = torch.tensor([local_t], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max = float(tt.item())
+    value = done_steps * world / t_max
+    kernel_rate = done_steps / local_t
+
+    # ---- end to end: host initial states in, host end states (+ rows) out ----
+    e2e = None
+    if not args.no_e2e and not graph_mode:
+        hin = [torch.from_numpy(np.ascontiguousarray(rays[k])).pin_memory()
+               for k in ("x0", "y0", "kx0", "ky0")]
+        hend = torch.empty_like(out.end_state, device="cpu").pin_memory()
+        hsaved = torch.empty_like(out.saved, device="cpu").pin_memory()
+        hsteps = torch.empty_like(out.n_steps, device="cpu").pin_memory()
+        hstat = torch.empty_like(out.status, device="cpu").pin_memory()
+        e2e_t = []
+        for i in range(args.steps + 1):
+            torch.cuda.synchronize()
+            t_a = time.perf_counter()
+            for d, h in zip(ins, hin):
+                d.copy_(h, non_blocking=True)
+            one(0)
+            hend.copy_(out.end_state, non_blocking=True)
+            hsteps.copy_(out.n_steps, non_blocking=True)
+            hstat.copy_(out.status, non_blocking=True)
+            if decimation:
+                hsaved.copy_(out.saved, non_blocking=True)
+            torch.cuda.synchronize()
+            if i:
+                e2e_t.append(time.perf_counter() - t_a)
+        e2e_steps = int(hsteps.to(torch.int64).sum().item())
+        e2e = {"value": e2e_steps * args.steps * world / sum(e2e_t), "unit": METRIC,
+               "h2d_bytes_per_step": 4 * n_all * 8,
+               "d2h_bytes_per_step": int(out.end_state.numel() * 8 + n_all * 5 +
+                                         (out.saved.numel() * 4 if decimation else 0)),
+               "path": "torch copies of page-locked host buffers around mr_batch_trace_device",
+               "ms_per_step": 1e3 * sum(e2e_t) / args.steps}
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+
+    # ---- the plain FP64 form on a subset of the same rays, and the error ----
+    # plain FP64 rate on a GPU-filling subset; errors on up to 4,096 of its rays
+    sub = int(min(n_all, 65536 if steps <= 4000 else 16384))
+    idx = np.sort(rng.choice(n_all, sub, replace=False))
+    scen_of = rays["scenario"][idx] if rays["scenario"] is not None else np.zeros(sub, np.uint8)
+    plain_steps, plain_time = 0, 0.0
+    errs_all = {"rel_position": [], "direction": [], "compared": 0, "n": 0}
+    ref_out = tracer.trace(*[t[torch.from_numpy(idx).to(dev)] for t in ins], dt, steps, t0=t0,
+                           scenario=(torch.from_numpy(scen_of).to(dev)
+                                     if rays["scenario"] is not None else None), config=cfg)
+    torch.cuda.synchronize()
+    end_sub = ref_out.end_state.cpu().numpy()
+    nst_sub = ref_out.n_steps.cpu().numpy()
+    for s_i, (b, c) in enumerate(handles):
+        m = np.nonzero(scen_of == s_i)[0]
+        if m.size == 0:
+            continue
+        sel = idx[m]
+        pin = [torch.from_numpy(np.ascontiguousarray(rays[k][sel])).to(dev)
+               for k in ("x0", "y0", "kx0", "ky0")]
+        traj = torch.empty((5, steps + 1, sel.size), dtype=torch.float64, device=dev)
+        nr = torch.empty(sel.size, dtype=torch.int32, device=dev)
+        st = torch.empty(sel.size, dtype=torch.uint8, device=dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        mr.trace_device(b, c, *pin, t0, t0 + steps * dt, dt, traj, nr, st, math="identity",
+                        stream=stream)
+        e1.record(stream)
+        e1.synchronize()
+        plain_time += e0.elapsed_time(e1) / 1e3
+        plain_steps += int((nr.to(torch.int64) - 1).sum().item())
+        k = min(m.size, max(1, 4096 // len(handles)))
+        er = endpoint_errors(end_sub[:, m[:k]], nst_sub[m[:k]], traj[:, :, :k].cpu().numpy(),
+                             nr[:k].cpu().numpy())
+        errs_all["rel_position"].append(er["rel_position"])
+        errs_all["direction"].append(er["direction"])
+        errs_all["compared"] += er["compared"]
+        errs_all["n"] += er["n"]
+        del traj
+    rel = np.concatenate(errs_all["rel_position"])
+    dth = np.concatenate(errs_all["direction"])
+    plain_rate = plain_steps / plain_time
+
+    L = mr._native.load()
+    fp32_peak = ctypes.c_double()
+    mr._native.check(L.mr_measure_fma_peak(0, ctypes.byref(fp32_peak)))
+    roofline = {"bound": "fp32", "achieved": None, "peak": fp32_peak.value, "unit": "TFLOP/s",
+                "frac": None, "peak_source": "measured: FP32 FMA-chain kernel on this GPU, this run",
+                "traffic": None}
+    if FP32_FLOP_PER_RAY_STEP:
+        ach = kernel_rate * FP32_FLOP_PER_RAY_STEP / 1e12
+        roofline.update({"achieved": ach, "frac": ach / fp32_peak.value,
+                         "flop_per_ray_step": FP32_FLOP_PER_RAY_STEP})
+    cpu = None
+    if not args.no_cpu_baseline and args.workload == "seamount":
+        threads = cpu_threads()
+        rate, desc, _ = cpu_sample(w, args.cpu_seconds, threads)
+        cpu = {"value": rate, "unit": METRIC, "cores": threads, "kind": "port", "sample": desc}
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": name, "form": "batched FP32 (rk4_f32), persistent, work queue",
+                   "rays_per_gpu": n_all, "max_steps": steps, "dt": dt, "decimation": decimation,
+                   "scenarios": len(handles), "launch": (tuned or cfg.as_dict()),
+                   "autotuned": tuned is not None, "graph_replay": graph_mode,
+                   "plain_fp64_same_rays": {"value": plain_rate, "unit": METRIC,
+                                            "rays": sub, "math": "identity"},
+                   "batched_over_plain": value / world / plain_rate,
+                   "endpoint_error_vs_fp64": {
+                       "rays": int(errs_all["compared"]), "of": int(errs_all["n"]),
+                       "rel_position_p50": float(np.median(rel)),
+                       "rel_position_p99": float(np.percentile(rel, 99)),
+                       "rel_position_max": float(rel.max()),
+                       "direction_p99_rad": float(np.percentile(dth, 99)),
+                       "direction_max_rad": float(dth.max())},
+                   "l2": "512 MB buffer written between timed steps",
+                   "parallelism": f"replicas x{world}"},
+        "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+        "clocks": clock,
+    }
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", 0))
@@ -373,6 +633,8 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", 0))
     if args.impl == "reference":
         reference_arm(args, rank, world)
+    elif args.form == "batched":
+        batched_arm(args, rank, world, local_rank)
     else:
         gb300_arm(args, rank, world, local_rank)
 
