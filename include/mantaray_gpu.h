@@ -263,6 +263,58 @@ int mr_batch_trace_device_static(mr_batch *b, size_t n, const uint8_t *ray_scena
                                  int32_t *n_saved, uint8_t *status,
                                  const mr_batch_config *cfg, void *stream);
 
+/* ---- differentiation form --------------------------------------------------
+ * Gradients of any function of the rays' end states with respect to the
+ * initial states (x, y, kx, ky) and every node of the depth, u and v grids:
+ * a hand-written discrete adjoint of the RK4 stepper (ode_solvers 0.4.0 as
+ * called at src/ray.rs:207-208) over the reference's equations
+ * (src/wave_ray_path.rs:118-216), with the grid lookups in the working
+ * precision and no f32 casts (the reference's casts make the map a staircase
+ * below any finite-difference step).  The forward pass stores every
+ * `checkpoint_every`-th state; the adjoint pass recomputes each segment from
+ * its checkpoint.  mr_diff_tangent is the forward-mode (tangent-linear)
+ * derivative of the same map, for checking.  precision: 64 (double arrays)
+ * or 32 (float arrays; node gradients are still accumulated in double).
+ * Fields are row-major [ny][nx] on regular grids; all arrays are device
+ * memory; calls are asynchronous on `stream`. */
+typedef struct mr_diff_grid {
+  size_t nx, ny;   /* points per axis, >= 2 */
+  double x0, y0;   /* first axis values */
+  double dx, dy;   /* spacing, > 0 */
+} mr_diff_grid;
+
+/* End states [4][n] (x, y, kx, ky) after `steps` steps of dt; status[i] = 1
+ * (and NaN) for rays that left the grids or met depth <= 0.  checkpoints:
+ * [ceil(steps / checkpoint_every)][4][n]. */
+int mr_diff_forward(int precision, const mr_diff_grid *bgrid, const void *depth,
+                    const mr_diff_grid *cgrid, const void *u, const void *v,
+                    size_t n, const void *x0, const void *y0, const void *kx0,
+                    const void *ky0, double dt, int64_t steps,
+                    int64_t checkpoint_every, void *checkpoints, void *end_state,
+                    uint8_t *status, void *stream);
+
+/* Given grad_end [4][n] = dL/d(end state), writes grad_state0 [4][n] =
+ * dL/d(initial state) and sets grad_depth [bny*bnx], grad_u, grad_v
+ * [cny*cnx] (f64) to dL/d(node).  Rays with status != 0 contribute nothing.
+ * segment: scratch [checkpoint_every][4][n]. */
+int mr_diff_backward(int precision, const mr_diff_grid *bgrid, const void *depth,
+                     const mr_diff_grid *cgrid, const void *u, const void *v,
+                     size_t n, const void *x0, const void *y0, const void *kx0,
+                     const void *ky0, double dt, int64_t steps,
+                     int64_t checkpoint_every, const void *checkpoints,
+                     const uint8_t *status, const void *grad_end, void *segment,
+                     void *grad_state0, double *grad_depth, double *grad_u,
+                     double *grad_v, void *stream);
+
+/* Directional derivative of the end states along dstate0 [4][n] and the
+ * node perturbations d_depth, d_u, d_v (each may be null): d_end [4][n]. */
+int mr_diff_tangent(int precision, const mr_diff_grid *bgrid, const void *depth,
+                    const mr_diff_grid *cgrid, const void *u, const void *v,
+                    size_t n, const void *x0, const void *y0, const void *kx0,
+                    const void *ky0, const void *dstate0, const void *d_depth,
+                    const void *d_u, const void *d_v, double dt, int64_t steps,
+                    void *end_state, void *d_end, uint8_t *status, void *stream);
+
 /* ---- NetCDF-3 access (host only, no GPU) ---------------------------------- */
 
 /* Reads variable `name` of a NetCDF-3 file converted to f64 (the reference's

@@ -36,7 +36,7 @@ SYMBOLS = (
     "mr_last_error", "mr_version", "mr_measure_fma_peak",
     "mr_batch_default_config", "mr_batch_create", "mr_batch_destroy", "mr_batch_trace_device",
     "mr_batch_graph_create", "mr_batch_graph_launch", "mr_batch_graph_destroy",
-    "mr_batch_trace_device_static",
+    "mr_batch_trace_device_static", "mr_diff_forward", "mr_diff_backward", "mr_diff_tangent",
 )
 
 BATCH_STATIC_MAX_SCENARIOS = 64
@@ -45,6 +45,13 @@ BATCH_COMPLETE = 0
 BATCH_OUT_OF_DOMAIN = 1
 BATCH_DRY = 2
 BATCH_BAD_WAVENUMBER = 3
+
+
+class DiffGrid(ctypes.Structure):
+    """mr_diff_grid: a regular grid (points, origin, spacing)."""
+
+    _fields_ = [("nx", ctypes.c_size_t), ("ny", ctypes.c_size_t), ("x0", ctypes.c_double),
+                ("y0", ctypes.c_double), ("dx", ctypes.c_double), ("dy", ctypes.c_double)]
 
 
 class BatchConfig(ctypes.Structure):
@@ -121,6 +128,13 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
                                         ctypes.c_int64, sz, vp, vp, vp, vp, vp, P(BatchConfig),
                                         pp]),
         "mr_batch_graph_launch": (i32, [vp, sz, vp]),
+        "mr_diff_forward": (i32, [i32, P(DiffGrid), vp, P(DiffGrid), vp, vp, sz, vp, vp, vp, vp,
+                                  f64, ctypes.c_int64, ctypes.c_int64, vp, vp, vp, vp]),
+        "mr_diff_backward": (i32, [i32, P(DiffGrid), vp, P(DiffGrid), vp, vp, sz, vp, vp, vp, vp,
+                                   f64, ctypes.c_int64, ctypes.c_int64, vp, vp, vp, vp, vp, vp,
+                                   vp, vp, vp]),
+        "mr_diff_tangent": (i32, [i32, P(DiffGrid), vp, P(DiffGrid), vp, vp, sz, vp, vp, vp, vp,
+                                  vp, vp, vp, vp, f64, ctypes.c_int64, vp, vp, vp, vp]),
         "mr_batch_trace_device_static": (i32, [vp, sz, vp, vp, vp, vp, vp, f64, f64,
                                                ctypes.c_int64, ctypes.c_int64, sz, vp, vp, vp,
                                                vp, vp, P(BatchConfig), vp]),

@@ -35,6 +35,7 @@ UNITS = {
     "rk4_f32.cu": ["-fmad=false"],
     "batch_api.cu": [],
     "batch_static.cu": [],
+    "diff.cu": [],
 }
 
 

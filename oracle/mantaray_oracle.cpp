@@ -599,3 +599,119 @@ int or_trace_final(const or_bathy *b, const or_current *c, size_t n,
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// The differentiation model: the reference's equations with the grid lookups
+// in f64 (no f32 casts), which makes the step map smooth inside each cell
+// (the f32 casts of the reference make it a staircase at the ulp level, below
+// any finite-difference step).  Same corner rule as the reference
+// (idx in [0, n-1], the last cell for idx == n-1), f64 bilinear, f64 cell
+// forward differences, and the reference's RHS expressions.  This is the
+// function the GPU adjoint and tangent-linear kernels differentiate; it is
+// here so finite differences of it can check them.
+
+namespace {
+
+struct Grid64 {
+  const double *v0, *v1;  // one or two fields on the grid
+  size_t nx, ny;
+  double x0, y0, dx, dy;
+};
+
+// Cell (i, j) and in-cell fractions of (x, y); false outside the grid.
+bool cell64(const Grid64 &g, double x, double y, size_t *i, size_t *j, double *fx, double *fy) {
+  const double ix = (x - g.x0) / g.dx, iy = (y - g.y0) / g.dy;
+  if (!(ix >= 0.0 && ix <= static_cast<double>(g.nx - 1) && iy >= 0.0 &&
+        iy <= static_cast<double>(g.ny - 1)))
+    return false;
+  double fi = std::floor(ix), fj = std::floor(iy);
+  if (fi > static_cast<double>(g.nx - 2)) fi = static_cast<double>(g.nx - 2);
+  if (fj > static_cast<double>(g.ny - 2)) fj = static_cast<double>(g.ny - 2);
+  *i = static_cast<size_t>(fi);
+  *j = static_cast<size_t>(fj);
+  *fx = ix - fi;
+  *fy = iy - fj;
+  return true;
+}
+
+inline double bilin64(const double *a, size_t nx, size_t i, size_t j, double fx, double fy,
+                      double *ddx, double *ddy) {
+  const double v00 = a[nx * j + i], v10 = a[nx * j + i + 1];
+  const double v01 = a[nx * (j + 1) + i], v11 = a[nx * (j + 1) + i + 1];
+  *ddx = v10 - v00;  // forward differences (divided by the spacing by the caller)
+  *ddy = v01 - v00;
+  return ((v00 + (v10 - v00) * fx) + (v01 - v00) * fy) + (((v11 - v10) - v01) + v00) * fx * fy;
+}
+
+int odes_f64interp(const Grid64 &bg, const Grid64 &cg, double x, double y, double kx, double ky,
+                   double out[4]) {
+  size_t i, j;
+  double fx, fy, gx, gy;
+  if (!cell64(bg, x, y, &i, &j, &fx, &fy)) return OR_INDEX_OUT_OF_BOUNDS;
+  const double h = bilin64(bg.v0, bg.nx, i, j, fx, fy, &gx, &gy);
+  const double hx = gx / bg.dx, hy = gy / bg.dy;
+  if (!cell64(cg, x, y, &i, &j, &fx, &fy)) return OR_INDEX_OUT_OF_BOUNDS;
+  double ux, uy, vx, vy;
+  const double u = bilin64(cg.v0, cg.nx, i, j, fx, fy, &ux, &uy);
+  const double v = bilin64(cg.v1, cg.nx, i, j, fx, fy, &vx, &vy);
+  ux /= cg.dx; uy /= cg.dy; vx /= cg.dx; vy /= cg.dy;
+  const double k = std::sqrt(kx * kx + ky * ky);
+  double cgv;
+  int e = group_velocity(k, h, &cgv);
+  if (e) return e;
+  double dkb[2];
+  dkdt_bathy(k, h, hx, hy, dkb);
+  out[0] = cgv * (kx / k) + u;
+  out[1] = cgv * (ky / k) + v;
+  out[2] = (dkb[0] - kx * ux) - ky * vx;
+  out[3] = (dkb[1] - kx * uy) - ky * vy;
+  return OR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int or_diff_end_states(const double *depth, size_t bnx, size_t bny, double bx0, double by0,
+                       double bdx, double bdy, const double *u, const double *v, size_t cnx,
+                       size_t cny, double cx0, double cy0, double cdx, double cdy, size_t n,
+                       const double *x0, const double *y0, const double *kx0, const double *ky0,
+                       double dt, uint64_t steps, double *end_state, uint8_t *status,
+                       int threads) {
+  if (bnx < 2 || bny < 2 || cnx < 2 || cny < 2) return -1;
+  const Grid64 bg{depth, nullptr, bnx, bny, bx0, by0, bdx, bdy};
+  const Grid64 cg{u, v, cnx, cny, cx0, cy0, cdx, cdy};
+#ifdef _OPENMP
+  if (threads <= 0) threads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 4) num_threads(threads)
+#endif
+  for (long long r = 0; r < static_cast<long long>(n); ++r) {
+    const size_t i = static_cast<size_t>(r);
+    double y[4] = {x0[i], y0[i], kx0[i], ky0[i]};
+    const double half = dt / 2.0, sixth = dt / 6.0;
+    bool ok = true;
+    auto f = [&](const double *s, double *d) {
+      if (odes_f64interp(bg, cg, s[0], s[1], s[2], s[3], d) != OR_OK) {
+        d[0] = d[1] = d[2] = d[3] = std::numeric_limits<double>::quiet_NaN();
+      }
+    };
+    for (uint64_t st = 0; st < steps && ok; ++st) {
+      double k1[4], k2[4], k3[4], k4[4], tmp[4];
+      f(y, k1);
+      for (int q = 0; q < 4; ++q) tmp[q] = y[q] + k1[q] * half;
+      f(tmp, k2);
+      for (int q = 0; q < 4; ++q) tmp[q] = y[q] + k2[q] * half;
+      f(tmp, k3);
+      for (int q = 0; q < 4; ++q) tmp[q] = y[q] + k3[q] * dt;
+      f(tmp, k4);
+      for (int q = 0; q < 4; ++q) y[q] = y[q] + (((k1[q] + k2[q] * 2.0) + k3[q] * 2.0) + k4[q]) * sixth;
+      if (std::isnan(y[0]) || std::isnan(y[1]) || std::isnan(y[2]) || std::isnan(y[3])) ok = false;
+    }
+    for (int q = 0; q < 4; ++q) end_state[q * n + i] = ok ? y[q] : std::numeric_limits<double>::quiet_NaN();
+    status[i] = ok ? OR_RAY_COMPLETE : OR_RAY_STOPPED;
+  }
+  (void)threads;
+  return 0;
+}
+
+}  // extern "C"

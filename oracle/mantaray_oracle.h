@@ -123,6 +123,18 @@ int or_trace_final(const or_bathy *b, const or_current *c, size_t n,
                    int stop_rule, double *final_state, int32_t *n_rows,
                    uint8_t *status, int threads);
 
+/* The differentiation model (f64 lookups, see the .cpp): end states [4][n]
+ * (x, y, kx, ky) after `steps` RK4 steps, NaN with status 1 for rays that
+ * met a NaN derivative.  Fields are raw row-major arrays [ny][nx] on grids
+ * with origin (x0, y0) and spacing (dx, dy).  Returns 0 or -1. */
+int or_diff_end_states(const double *depth, size_t bnx, size_t bny, double bx0,
+                       double by0, double bdx, double bdy, const double *u,
+                       const double *v, size_t cnx, size_t cny, double cx0,
+                       double cy0, double cdx, double cdy, size_t n,
+                       const double *x0, const double *y0, const double *kx0,
+                       const double *ky0, double dt, uint64_t steps,
+                       double *end_state, uint8_t *status, int threads);
+
 #ifdef __cplusplus
 }
 #endif

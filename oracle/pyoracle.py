@@ -89,6 +89,10 @@ def lib() -> ctypes.CDLL:
     L.or_trace_final.restype = i32
     L.or_trace_final.argtypes = [vp, vp, sz, P(f64), P(f64), P(f64), P(f64), f64, f64, f64,
                                  i32, P(f64), P(ctypes.c_int32), P(ctypes.c_uint8), i32]
+    L.or_diff_end_states.restype = i32
+    L.or_diff_end_states.argtypes = [P(f64), sz, sz, f64, f64, f64, f64, P(f64), P(f64), sz, sz,
+                                     f64, f64, f64, f64, sz, P(f64), P(f64), P(f64), P(f64), f64,
+                                     ctypes.c_uint64, P(f64), P(ctypes.c_uint8), i32]
     _lib = L
     return L
 
@@ -262,3 +266,24 @@ def trace_final(bathy, current, x0, y0, kx0, ky0, t0, t_end, dt, stop_rule=STOP_
                          _ptr(final, ctypes.c_double), _ptr(n_rows, ctypes.c_int32),
                          _ptr(status, ctypes.c_uint8), threads)
     return final, n_rows, status
+
+
+def diff_end_states(depth, bgeom, u, v, cgeom, x0, y0, kx0, ky0, dt, steps, threads=0):
+    """End states [4][n] of the differentiation model (f64 lookups).
+    bgeom/cgeom = (x0, y0, dx, dy); depth, u, v shaped [ny][nx]."""
+    depth = np.ascontiguousarray(depth, dtype=np.float64)
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    v = np.ascontiguousarray(v, dtype=np.float64)
+    x0, y0, kx0, ky0 = (np.ascontiguousarray(np.atleast_1d(a), dtype=np.float64)
+                        for a in (x0, y0, kx0, ky0))
+    n = x0.size
+    end = np.empty((4, n), np.float64)
+    status = np.zeros(n, np.uint8)
+    d = ctypes.c_double
+    rc = lib().or_diff_end_states(
+        _ptr(depth, d), depth.shape[1], depth.shape[0], *bgeom, _ptr(u, d), _ptr(v, d), u.shape[1],
+        u.shape[0], *cgeom, n, _ptr(x0, d), _ptr(y0, d), _ptr(kx0, d), _ptr(ky0, d), dt, steps,
+        _ptr(end, d), _ptr(status, ctypes.c_uint8), threads)
+    if rc != 0:
+        raise ValueError("grids need at least 2 x 2 points")
+    return end, status

@@ -1,0 +1,195 @@
+"""The differentiation form on the GPU: tangent-linear kernel against central
+finite differences of the same model run by the CPU oracle, adjoint against
+the tangent-linear kernel (dot-product test), adjoint node gradients against
+finite differences on seeded nodes (delta h = 1e-3 m), the FP32 adjoint
+against the FP64 one, and the torch.autograd.Function.
+
+Bars: TLM vs FD <= 1e-5 relative; adjoint vs TLM <= 1e-10 relative; adjoint
+vs FD on nodes <= 1e-5 relative (FP64)."""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def case():
+    import torch
+
+    from mantaray_gb300.diff import grid
+    from mantaray_gb300.workloads import shelf_bump
+
+    w = shelf_bump(n_rays=512, steps=3000)
+    target = shelf_bump(n_rays=512, steps=3000, bump_scale=1.1)
+    g = grid(512, 512, 0.0, 0.0, 200.0, 200.0)
+    dev = torch.device("cuda")
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)  # noqa: E731
+    return {"w": w, "target": target, "g": g, "geom": (0.0, 0.0, 200.0, 200.0),
+            "rays": [t(a) for a in (w.x0, w.y0, w.kx0, w.ky0)],
+            "depth": t(w.depth), "u": t(w.u), "v": t(w.v), "t_depth": t(target.depth),
+            "steps": 3000, "dt": 1.0}
+
+
+def _oracle_end(oracle, case, depth=None, u=None, v=None, rays=None, idx=None):
+    w = case["w"]
+    r = rays if rays is not None else (w.x0, w.y0, w.kx0, w.ky0)
+    if idx is not None:
+        r = [a[idx] for a in r]
+    end, st = oracle.diff_end_states(w.depth if depth is None else depth, case["geom"],
+                                     w.u if u is None else u, w.v if v is None else v,
+                                     case["geom"], *r, case["dt"], case["steps"])
+    return end, st
+
+
+def test_forward_matches_oracle_model(oracle, case):
+    from mantaray_gb300.diff import ray_endpoints
+
+    end, status = ray_endpoints(*case["rays"], case["depth"], case["u"], case["v"], case["g"],
+                                case["g"], case["dt"], case["steps"])
+    o_end, o_st = _oracle_end(oracle, case)
+    st = status.cpu().numpy()
+    np.testing.assert_array_equal(st, o_st)
+    e = end.detach().cpu().numpy()
+    ok = st == 0
+    assert ok.sum() > 400
+    scale = np.maximum(np.abs(o_end[:, ok]), np.array([[1.0], [1.0], [1e-6], [1e-6]]))
+    assert float(np.max(np.abs(e[:, ok] - o_end[:, ok]) / scale)) <= 1e-9
+
+
+def test_tangent_matches_finite_differences(oracle, case):
+    import torch
+
+    from mantaray_gb300.diff import tangent
+
+    w = case["w"]
+    rng = np.random.default_rng(31)
+    n = w.n
+    # initial-state direction, a smooth depth bump, a smooth u perturbation
+    X, Y = np.meshgrid(np.arange(512) * 200.0, np.arange(512) * 200.0)
+    blob = np.exp(-((X - 20000.0) ** 2 + (Y - 50000.0) ** 2) / (2 * 6000.0 ** 2))
+    ds0 = np.stack([rng.normal(0, 1.0, n), rng.normal(0, 1.0, n), rng.normal(0, 1e-4, n),
+                    rng.normal(0, 1e-4, n)])
+    cases = [("state", ds0, None, None), ("depth", np.zeros((4, n)), 50.0 * blob, None),
+             ("u", np.zeros((4, n)), None, 0.1 * blob)]
+    dev = case["depth"].device
+    for name, dst, dd, du in cases:
+        end, d_end, st = tangent(*case["rays"], case["depth"], case["u"], case["v"], case["g"],
+                                 case["g"], case["dt"], case["steps"],
+                                 dstate0=torch.from_numpy(dst).to(dev),
+                                 d_depth=None if dd is None else torch.from_numpy(dd).to(dev),
+                                 d_u=None if du is None else torch.from_numpy(du).to(dev))
+        d_end = d_end.cpu().numpy()
+        st = st.cpu().numpy()
+        eps = 1e-4
+        rays_p = [a + eps * dst[q] for q, a in enumerate((w.x0, w.y0, w.kx0, w.ky0))]
+        rays_m = [a - eps * dst[q] for q, a in enumerate((w.x0, w.y0, w.kx0, w.ky0))]
+        ep, sp = _oracle_end(oracle, case, depth=None if dd is None else w.depth + eps * dd,
+                             u=None if du is None else w.u + eps * du, rays=rays_p)
+        em, sm = _oracle_end(oracle, case, depth=None if dd is None else w.depth - eps * dd,
+                             u=None if du is None else w.u - eps * du, rays=rays_m)
+        fd = (ep - em) / (2 * eps)
+        ok = (st == 0) & (sp == 0) & (sm == 0)
+        assert ok.sum() > 400, name
+        for q, floor in enumerate((1e-3, 1e-3, 1e-9, 1e-9)):
+            a, b = d_end[q, ok], fd[q, ok]
+            rel = np.abs(a - b) / np.maximum(np.abs(b), floor)
+            # a few rays cross a cell edge between the +/- runs (the map is
+            # only piecewise smooth); the bar holds for 99% of rays
+            assert np.percentile(rel, 99) <= 1e-5, (name, q, float(np.percentile(rel, 99)))
+
+
+def test_adjoint_dot_product(case):
+    import torch
+
+    from mantaray_gb300.diff import ray_endpoints, tangent
+
+    rng = np.random.default_rng(41)
+    dev = case["depth"].device
+    n = case["w"].n
+    rays = [r.clone().requires_grad_(True) for r in case["rays"]]
+    depth = case["depth"].clone().requires_grad_(True)
+    u = case["u"].clone().requires_grad_(True)
+    v = case["v"].clone().requires_grad_(True)
+    end, status = ray_endpoints(*rays, depth, u, v, case["g"], case["g"], case["dt"],
+                                case["steps"])
+    ok = status == 0
+    wgt = torch.from_numpy(rng.normal(size=(4, n)) * np.array([[1e-3], [1e-3], [10.0], [10.0]])).to(dev)
+    wgt = torch.where(ok, wgt, torch.zeros_like(wgt))
+    (torch.where(ok, end, torch.zeros_like(end)) * wgt).sum().backward()
+    ds0 = rng.normal(size=(4, n)) * np.array([[1.0], [1.0], [1e-4], [1e-4]])
+    dD = rng.normal(size=(512, 512)) * 0.5
+    dU = rng.normal(size=(512, 512)) * 1e-3
+    dV = rng.normal(size=(512, 512)) * 1e-3
+    t = lambda a: torch.from_numpy(a).to(dev)  # noqa: E731
+    _, d_end, st = tangent(*case["rays"], case["depth"], case["u"], case["v"], case["g"], case["g"],
+                           case["dt"], case["steps"], dstate0=t(ds0), d_depth=t(dD), d_u=t(dU),
+                           d_v=t(dV))
+    lhs = float((torch.where(ok, d_end, torch.zeros_like(d_end)) * wgt).sum())
+    rhs = (sum(float((r.grad * t(ds0[q])).sum()) for q, r in enumerate(rays)) +
+           float((depth.grad * t(dD)).sum()) + float((u.grad * t(dU)).sum()) +
+           float((v.grad * t(dV)).sum()))
+    assert abs(lhs - rhs) <= 1e-10 * max(abs(lhs), abs(rhs)), (lhs, rhs)
+
+
+def test_adjoint_node_gradients_against_finite_differences(oracle, case):
+    # the differentiation case's loss against targets traced over the same
+    # field with the bump raised 10%; FD on 64 seeded depth nodes, dh = 1e-3 m
+    import torch
+
+    from mantaray_gb300.diff import endpoint_loss, ray_endpoints
+
+    w = case["w"]
+    tgt, tst = ray_endpoints(*case["rays"], case["t_depth"], case["u"], case["v"], case["g"],
+                             case["g"], case["dt"], case["steps"])
+    y_t, th_t = tgt[1].detach(), torch.atan2(tgt[3], tgt[2]).detach()
+    depth = case["depth"].clone().requires_grad_(True)
+    end, status = ray_endpoints(*case["rays"], depth, case["u"], case["v"], case["g"], case["g"],
+                                case["dt"], case["steps"])
+    keep = (status == 0) & (tst == 0)
+    loss = endpoint_loss(end, torch.where(keep, status, torch.ones_like(status)), y_t, th_t)
+    loss.backward()
+    grad = depth.grad.cpu().numpy()
+    keep_np = keep.cpu().numpy()
+    y_np, th_np = y_t.cpu().numpy(), th_t.cpu().numpy()
+
+    def oracle_loss(dep):
+        e, s = _oracle_end(oracle, case, depth=dep)
+        m = keep_np & (s == 0)
+        th = np.arctan2(e[3], e[2])
+        return float(np.sum((e[1, m] - y_np[m]) ** 2 + (th[m] - th_np[m]) ** 2))
+
+    rng = np.random.default_rng(51)
+    cand = np.argwhere(np.abs(grad) > 1e-3 * np.abs(grad).max())
+    nodes = cand[rng.choice(len(cand), 64, replace=False)]
+    rel = []
+    for j, i in nodes:
+        dp = w.depth.copy(); dp[j, i] += 1e-3
+        dm = w.depth.copy(); dm[j, i] -= 1e-3
+        fd = (oracle_loss(dp) - oracle_loss(dm)) / 2e-3
+        rel.append(abs(grad[j, i] - fd) / max(abs(fd), 1e-12))
+    rel = np.array(rel)
+    assert np.median(rel) <= 1e-6 and np.percentile(rel, 90) <= 1e-5, rel
+
+
+def test_fp32_adjoint_follows_fp64(case):
+    import torch
+
+    from mantaray_gb300.diff import ray_endpoints
+
+    grads = {}
+    for dt_ in (torch.float64, torch.float32):
+        rays = [r.to(dt_).clone().requires_grad_(True) for r in case["rays"]]
+        depth = case["depth"].to(dt_).clone().requires_grad_(True)
+        end, status = ray_endpoints(*rays, depth, case["u"].to(dt_), case["v"].to(dt_), case["g"],
+                                    case["g"], case["dt"], case["steps"])
+        ok = status == 0
+        torch.where(ok, end[1], torch.zeros_like(end[1])).sum().backward()
+        grads[dt_] = (depth.grad.double().cpu().numpy(), rays[2].grad.double().cpu().numpy(),
+                      end.detach().double().cpu().numpy(), ok.cpu().numpy())
+    g64, g32 = grads[torch.float64], grads[torch.float32]
+    ok = g64[3] & g32[3]
+    assert ok.sum() > 400
+    assert np.max(np.abs(g32[2][1, ok] - g64[2][1, ok]) / np.abs(g64[2][1, ok])) <= 1e-4
+    num = np.linalg.norm(g32[0] - g64[0])
+    assert num <= 1e-2 * np.linalg.norm(g64[0])
