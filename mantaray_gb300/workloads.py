@@ -93,25 +93,27 @@ def shelf_bump(n_rays: int = 262144, steps: int = 3000, bump_scale: float = 1.0,
                seed: int = 1002) -> Workload:
     """Differentiation case: 262,144 rays on a 512 x 512 grid at 200 m.
     Bathymetry: a linear shelf from 3,000 m (x = 0) to 20 m (far edge) with a
-    1,500 m Gaussian shoal (sigma 8 km) at (30 km, 51.2 km), floored at 5 m;
+    1,500 m Gaussian shoal (sigma 8 km) at the centre of the domain, where the
+    shelf is 1,510 m deep (so its top is at 10 m), floored at 5 m;
     `bump_scale` multiplies the shoal (1.1 gives the loss targets).  Current:
     a Gaussian jet u(y) = 1.0 exp(-(y - 51.2 km)^2 / (2 (5 km)^2)), v = 0.
-    Rays from x = 0, y ~ U[10, 92] km, directions ~ U(+-30 deg), T ~ U[8, 14] s;
-    dt = 1 s for 3,000 steps."""
+    Rays start at x = 25 km, y ~ U[25, 77] km, directions ~ U(+-30 deg),
+    T ~ U[8, 14] s, so that in 3,000 s they cross the shoal; dt = 1 s."""
     rng = np.random.default_rng(seed)
     n = 512
     x = np.arange(n, dtype=np.float64) * 200.0
     L = x[-1]
     shelf = 3000.0 - 2980.0 * (x / L)
-    r2 = (x[None, :] - 30000.0) ** 2 + (x[:, None] - 51200.0) ** 2
+    r2 = (x[None, :] - 51200.0) ** 2 + (x[:, None] - 51200.0) ** 2
     depth = np.maximum(5.0, shelf[None, :] - bump_scale * 1500.0 * np.exp(-r2 / (2.0 * 8000.0 ** 2)))
     u = np.broadcast_to(np.exp(-((x[:, None] - 51200.0) ** 2) / (2.0 * 5000.0 ** 2)), (n, n)).copy()
     v = np.zeros((n, n))
-    y0 = rng.uniform(10000.0, 92000.0, n_rays)
+    y0 = rng.uniform(25000.0, 77000.0, n_rays)
     theta = rng.uniform(-np.deg2rad(30.0), np.deg2rad(30.0), n_rays)
     period = rng.uniform(8.0, 14.0, n_rays)
-    x0 = np.zeros(n_rays)
-    kx0, ky0 = wavenumber_vector(period, np.full(n_rays, 3000.0), theta)
+    x0 = np.full(n_rays, 25000.0)
+    h0 = 3000.0 - 2980.0 * (x0 / L)
+    kx0, ky0 = wavenumber_vector(period, h0, theta)
     return Workload(f"shelf_bump_{n_rays}rays_512x512_dt1_{steps}steps", x.astype(np.float32),
                     x.astype(np.float32), depth, x, x, u, v, x0, y0, kx0, ky0, 0.0, float(steps),
                     1.0, {"grid": (n, n), "spacing": 200.0, "bump_scale": bump_scale})
