@@ -65,8 +65,11 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--math", default="identity", choices=["identity", "libm"],
                    help="right-hand-side arithmetic of the plain FP64 kernel")
-    p.add_argument("--form", default="plain", choices=["plain", "batched"],
-                   help="plain FP64 drop-in (default) or the batched FP32 form")
+    p.add_argument("--form", default="plain", choices=["plain", "batched", "adjoint"],
+                   help="plain FP64 drop-in (default), the batched FP32 form, or the "
+                        "differentiation form (adjoint vs forward time)")
+    p.add_argument("--precision", type=int, default=64, choices=[64, 32],
+                   help="adjoint form: FP64 or FP32 arithmetic")
     p.add_argument("--workload", default="seamount",
                    choices=["seamount", "shelf_slope", "multi_source"],
                    help="batched form only: the seamount case, the 8192^2 shelf-slope case "
@@ -626,6 +629,103 @@ def batched_arm(args, rank: int, world: int, local_rank: int):
         dist.destroy_process_group()
 
 
+def adjoint_arm(args, rank: int, world: int, local_rank: int):
+    """The differentiation case: gradient of the endpoint loss with respect to
+    the initial states and every depth / current node for 262,144 rays x
+    3,000 steps (checkpoints every 55 steps), against the forward pass."""
+    import torch
+
+    import mantaray_gb300 as mr
+    from mantaray_gb300.diff import endpoint_loss, grid, ray_endpoints
+    from mantaray_gb300.workloads import shelf_bump
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    n_rays = args.rays if args.rays != 65536 else 262144
+    steps = args.trace_steps if args.trace_steps != 4000 else 3000
+    w = shelf_bump(n_rays=n_rays, steps=steps)
+    tg = shelf_bump(n_rays=n_rays, steps=steps, bump_scale=1.1)
+    dtype = torch.float64 if args.precision == 64 else torch.float32
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev).to(dtype)  # noqa: E731
+    g = grid(512, 512, 0.0, 0.0, 200.0, 200.0)
+    rays = [t(a) for a in (w.x0, w.y0, w.kx0, w.ky0)]
+    D, U, V = t(w.depth), t(w.u), t(w.v)
+    every = 55
+    tgt, tst = ray_endpoints(*rays, t(tg.depth), U, V, g, g, 1.0, steps, every)
+    y_t, th_t = tgt[1], torch.atan2(tgt[3], tgt[2])
+    stream = torch.cuda.current_stream(dev)
+
+    def forward_only():
+        with torch.no_grad():
+            return ray_endpoints(*rays, D, U, V, g, g, 1.0, steps, every)
+
+    def gradient():
+        depth = D.clone().requires_grad_(True)
+        u = U.clone().requires_grad_(True)
+        v = V.clone().requires_grad_(True)
+        r = [x.clone().requires_grad_(True) for x in rays]
+        end, status = ray_endpoints(*r, depth, u, v, g, g, 1.0, steps, every)
+        keep = (status == 0) & (tst == 0)
+        loss = endpoint_loss(end, torch.where(keep, status, torch.ones_like(status)), y_t, th_t)
+        loss.backward()
+        return loss
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(args.steps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1) / 1e3)
+        return sum(ts) / len(ts)
+
+    with ClockSampler(local_rank) as clocks:
+        t_fwd = timed(forward_only)
+        t_grad = timed(gradient)
+    clock = clocks.summary()
+    # the plain FP64 drop-in kernel over the same rays and fields (f32-cast
+    # lookups, as the reference), for scale
+    b = mr.Bathymetry.grid(w.bx, w.by, w.depth)
+    c = mr.Current.grid(w.cx, w.cy, w.u, w.v)
+    sub = min(n_rays, 65536)
+    pin = [torch.from_numpy(a[:sub]).to(dev) for a in (w.x0, w.y0, w.kx0, w.ky0)]
+    traj = torch.empty((5, steps + 1, sub), dtype=torch.float64, device=dev)
+    nr = torch.empty(sub, dtype=torch.int32, device=dev)
+    st = torch.empty(sub, dtype=torch.uint8, device=dev)
+
+    def plain():
+        mr.trace_device(b, c, *pin, 0.0, float(steps), 1.0, traj, nr, st, math="identity",
+                        stream=stream)
+
+    t_plain = timed(plain) * n_rays / sub
+    ray_steps = n_rays * steps
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": ray_steps / t_grad, "unit": METRIC, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_grad,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == 64 else "f32", "data": "synthetic",
+        "config": {"workload": w.name, "form": "differentiation: forward with checkpoints + "
+                                               "discrete adjoint (mr_diff_*)",
+                   "rays": n_rays, "steps_per_ray": steps, "checkpoint_every": every,
+                   "gradient_ms": 1e3 * t_grad, "forward_ms": 1e3 * t_fwd,
+                   "plain_fp64_forward_ms": 1e3 * t_plain,
+                   "gradient_over_forward": t_grad / t_fwd,
+                   "gradient_over_plain_forward": t_grad / t_plain,
+                   "value_is": "ray-steps of the traced rays per second of a full gradient"},
+        "roofline": None, "cpu_baseline": None, "e2e": None, "gpu_launches": 2 * args.steps,
+        "clocks": clock,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", 0))
@@ -635,6 +735,8 @@ def main():
         reference_arm(args, rank, world)
     elif args.form == "batched":
         batched_arm(args, rank, world, local_rank)
+    elif args.form == "adjoint":
+        adjoint_arm(args, rank, world, local_rank)
     else:
         gb300_arm(args, rank, world, local_rank)
 

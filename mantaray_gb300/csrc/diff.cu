@@ -28,6 +28,8 @@
 // backward.  Gradients with respect to grid nodes are accumulated per ray
 // while the ray stays in one cell, then added to the node arrays with FP64
 // atomics, aggregated across the lanes of a warp that flush the same cell.
+// The per-cell accumulation runs in the working precision; only the
+// accumulation onto the node arrays is FP64.
 
 #include <cuda_runtime.h>
 #include <math.h>
@@ -236,33 +238,37 @@ __device__ __forceinline__ void jvp(const DiffArgs<T> &A, const T s[4], const Po
 // ---------------------------------------------------------------- VJP --
 
 // Per-ray accumulator of node gradients for one bathymetry cell and one
-// current cell; flushed to the node arrays when the ray moves on.
+// current cell, in the working precision; flushed to the FP64 node arrays
+// when the ray moves on.
+template <typename T>
 struct NodeAcc {
   int64_t bkey, ckey;   // flat index of the cells' south-west nodes, -1: empty
-  double d[4];          // depth nodes (00, 10, 01, 11)
-  double u[4], v[4];
+  T d[4];               // depth nodes (00, 10, 01, 11)
+  T u[4], v[4];
 };
 
-// Adds `vals[4]` to nodes (base, base+1, base+nx, base+nx+1) of `arr`, summed
-// first across the active lanes of the warp that flush the same base.
-__device__ __forceinline__ void scatter4(double *arr, int64_t base, int nx, const double vals[4]) {
+// Adds `vals[4]` to nodes (base, base+1, base+nx, base+nx+1) of `arr` in
+// FP64, summed first across the active lanes of the warp that flush the same
+// base.
+template <typename T>
+__device__ __forceinline__ void scatter4(double *arr, int64_t base, int nx, const T vals[4]) {
   const unsigned active = __activemask();
   const unsigned peers = __match_any_sync(active, base);
   const int lane = threadIdx.x & 31;
   const int leader = __ffs(peers) - 1;
   const bool shared = __any_sync(active, __popc(peers) > 1);
-  double v[4] = {vals[0], vals[1], vals[2], vals[3]};
+  double v[4] = {double(vals[0]), double(vals[1]), double(vals[2]), double(vals[3])};
   if (shared) {
     // every active lane takes part in each shuffle; a group's leader keeps
     // the values of its peers
     for (int src = 0; src < 32; ++src) {
       if (!((active >> src) & 1u)) continue;
-      double o[4];
+      T o[4];
 #pragma unroll
       for (int q = 0; q < 4; ++q) o[q] = __shfl_sync(active, vals[q], src);
       if (lane == leader && src != lane && ((peers >> src) & 1u)) {
 #pragma unroll
-        for (int q = 0; q < 4; ++q) v[q] += o[q];
+        for (int q = 0; q < 4; ++q) v[q] += double(o[q]);
       }
     }
   }
@@ -275,28 +281,28 @@ __device__ __forceinline__ void scatter4(double *arr, int64_t base, int nx, cons
 }
 
 template <typename T>
-__device__ __forceinline__ void flush_bathy(const DiffArgs<T> &A, NodeAcc &acc) {
+__device__ __forceinline__ void flush_bathy(const DiffArgs<T> &A, NodeAcc<T> &acc) {
   if (acc.bkey >= 0) scatter4(A.grad_depth, acc.bkey, A.bg.nx, acc.d);
   acc.bkey = -1;
 #pragma unroll
-  for (int q = 0; q < 4; ++q) acc.d[q] = 0.0;
+  for (int q = 0; q < 4; ++q) acc.d[q] = T(0);
 }
 
 template <typename T>
-__device__ __forceinline__ void flush_current(const DiffArgs<T> &A, NodeAcc &acc) {
+__device__ __forceinline__ void flush_current(const DiffArgs<T> &A, NodeAcc<T> &acc) {
   if (acc.ckey >= 0) {
     scatter4(A.grad_u, acc.ckey, A.cg.nx, acc.u);
     scatter4(A.grad_v, acc.ckey, A.cg.nx, acc.v);
   }
   acc.ckey = -1;
 #pragma unroll
-  for (int q = 0; q < 4; ++q) acc.u[q] = acc.v[q] = 0.0;
+  for (int q = 0; q < 4; ++q) acc.u[q] = acc.v[q] = T(0);
 }
 
 // r = J(s)^T w, and the node gradients of w . F added to acc.
 template <typename T>
 __device__ __forceinline__ void vjp(const DiffArgs<T> &A, const T s[4], const Point<T> &P,
-                                    const T w[4], T r[4], NodeAcc &acc) {
+                                    const T w[4], T r[4], NodeAcc<T> &acc) {
   const T c = P.c, sn = P.s, k = P.k;
   const T g_h = (w[0] * c + w[1] * sn) * P.q_h + (w[2] * P.h.gx + w[3] * P.h.gy) * P.f_h;
   r[0] = P.h.dxp * g_h + w[0] * P.u.dxp + w[1] * P.v.dxp;
@@ -313,13 +319,12 @@ __device__ __forceinline__ void vjp(const DiffArgs<T> &A, const T s[4], const Po
       flush_bathy(A, acc);
       acc.bkey = key;
     }
-    const double fx = P.cb.fx, fy = P.cb.fy;
-    const double gh = g_h, hxw = double(w[2]) * P.f * A.bg.inv_dx,
-                 hyw = double(w[3]) * P.f * A.bg.inv_dy;
-    acc.d[0] += gh * (1.0 - fx) * (1.0 - fy) - hxw - hyw;
-    acc.d[1] += gh * fx * (1.0 - fy) + hxw;
-    acc.d[2] += gh * (1.0 - fx) * fy + hyw;
-    acc.d[3] += gh * fx * fy;
+    const T fx = P.cb.fx, fy = P.cb.fy;
+    const T hxw = w[2] * P.f * A.bg.inv_dx, hyw = w[3] * P.f * A.bg.inv_dy;
+    acc.d[0] += g_h * (T(1) - fx) * (T(1) - fy) - hxw - hyw;
+    acc.d[1] += g_h * fx * (T(1) - fy) + hxw;
+    acc.d[2] += g_h * (T(1) - fx) * fy + hyw;
+    acc.d[3] += g_h * fx * fy;
   }
   // current nodes of the cell
   {
@@ -328,12 +333,12 @@ __device__ __forceinline__ void vjp(const DiffArgs<T> &A, const T s[4], const Po
       flush_current(A, acc);
       acc.ckey = key;
     }
-    const double fx = P.cc.fx, fy = P.cc.fy;
-    const double w00 = (1.0 - fx) * (1.0 - fy), w10 = fx * (1.0 - fy), w01 = (1.0 - fx) * fy,
-                 w11 = fx * fy;
-    const double ix = A.cg.inv_dx, iy = A.cg.inv_dy;
-    const double kxw2 = double(s[2]) * w[2] * ix, kxw3 = double(s[2]) * w[3] * iy;
-    const double kyw2 = double(s[3]) * w[2] * ix, kyw3 = double(s[3]) * w[3] * iy;
+    const T fx = P.cc.fx, fy = P.cc.fy;
+    const T w00 = (T(1) - fx) * (T(1) - fy), w10 = fx * (T(1) - fy), w01 = (T(1) - fx) * fy,
+            w11 = fx * fy;
+    const T ix = A.cg.inv_dx, iy = A.cg.inv_dy;
+    const T kxw2 = s[2] * w[2] * ix, kxw3 = s[2] * w[3] * iy;
+    const T kyw2 = s[3] * w[2] * ix, kyw3 = s[3] * w[3] * iy;
     acc.u[0] += w[0] * w00 + kxw2 + kxw3;
     acc.u[1] += w[0] * w10 - kxw2;
     acc.u[2] += w[0] * w01 - kxw3;
@@ -423,10 +428,10 @@ __global__ void __launch_bounds__(64) diff_adjoint_kernel(DiffArgs<T> A) {
   T lam[4];
 #pragma unroll
   for (int q = 0; q < 4; ++q) lam[q] = A.grad_end[q * A.n + i];
-  NodeAcc acc;
+  NodeAcc<T> acc;
   acc.bkey = acc.ckey = -1;
 #pragma unroll
-  for (int q = 0; q < 4; ++q) acc.d[q] = acc.u[q] = acc.v[q] = 0.0;
+  for (int q = 0; q < 4; ++q) acc.d[q] = acc.u[q] = acc.v[q] = T(0);
   const T half = A.dt * T(0.5), h = A.dt;
   for (int64_t seg = A.n_ck - 1; seg >= 0; --seg) {
     const int64_t first = seg * A.ck_every;
