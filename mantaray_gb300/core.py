@@ -62,6 +62,24 @@ class TraceResult:
         """Ray i as the reference's list of (t, x, y, kx, ky) rows."""
         return np.ascontiguousarray(self.traj[:, : self.n_rows[i], i].T)
 
+    def ray_result(self, i: int) -> dict:
+        """Ray i as the reference's RayResult (src/ray_result.rs:123-150)."""
+        from . import results
+
+        return results.ray_result(self.ray(i))
+
+    def as_json(self, i: int) -> str:
+        """Ray i serialised as RayResult::as_json (src/ray_result.rs:74-76)."""
+        from . import results
+
+        return results.as_json(self.ray_result(i))
+
+    def append_tsv(self, path, i: int) -> None:
+        """Ray i appended to a TSV file as src/ray.rs:219-243 writes it."""
+        from . import results
+
+        results.append_tsv(path, self.ray(i))
+
 
 def _f64(a):
     return np.ascontiguousarray(np.atleast_1d(np.asarray(a, dtype=np.float64)))
