@@ -116,6 +116,16 @@ def cpu_sample(w, seconds: float, threads: int):
     return ray_steps / elapsed, desc, elapsed
 
 
+def cpu_baseline(w, seconds: float) -> dict:
+    """The cpu_baseline object: the oracle on all host cores for `seconds`,
+    and on one core for a quarter of that (value_1thread)."""
+    threads = cpu_threads()
+    rate, desc, _ = cpu_sample(w, seconds, threads)
+    rate1, desc1, _ = cpu_sample(w, max(seconds / 4.0, 1.0), 1)
+    return {"value": rate, "unit": METRIC, "cores": threads, "kind": "port", "sample": desc,
+            "value_1thread": rate1, "sample_1thread": desc1}
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
 
@@ -367,9 +377,7 @@ def gb300_arm(args, rank: int, world: int, local_rank: int):
 
     cpu = None
     if not args.no_cpu_baseline:
-        threads = cpu_threads()
-        rate, desc, _ = cpu_sample(w, args.cpu_seconds, threads)
-        cpu = {"value": rate, "unit": METRIC, "cores": threads, "kind": "port", "sample": desc}
+        cpu = cpu_baseline(w, args.cpu_seconds)
 
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
@@ -598,9 +606,7 @@ def batched_arm(args, rank: int, world: int, local_rank: int):
                          "flop_per_ray_step": FP32_FLOP_PER_RAY_STEP})
     cpu = None
     if not args.no_cpu_baseline and args.workload == "seamount":
-        threads = cpu_threads()
-        rate, desc, _ = cpu_sample(w, args.cpu_seconds, threads)
-        cpu = {"value": rate, "unit": METRIC, "cores": threads, "kind": "port", "sample": desc}
+        cpu = cpu_baseline(w, args.cpu_seconds)
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
