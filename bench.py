@@ -46,9 +46,9 @@ FP32_FLOP_PER_RAY_STEP = 541.7
 # DFMA = 2), per right-hand-side arithmetic, counted by ncu on the plain
 # kernel over the seamount workload
 # (sm__sass_thread_inst_executed_op_d{add,mul,fma}_pred_on; profiles/).
-FP64_FLOP_PER_RAY_STEP = {"libm": 1840.0, "identity": 384.0}
+FP64_FLOP_PER_RAY_STEP = {"libm": 1807.7, "identity": 339.0}
 # FP64-pipe instructions per ray-step (sm__inst_executed_pipe_fp64 x 32, same captures)
-FP64_PIPE_INST_PER_RAY_STEP = {"libm": 1317.0, "identity": 448.0}
+FP64_PIPE_INST_PER_RAY_STEP = {"libm": 1218.4, "identity": 276.3}
 
 
 def parse():
@@ -71,10 +71,11 @@ def parse():
     p.add_argument("--precision", type=int, default=64, choices=[64, 32],
                    help="adjoint form: FP64 or FP32 arithmetic")
     p.add_argument("--workload", default="seamount",
-                   choices=["seamount", "shelf_slope", "multi_source"],
-                   help="batched form only: the seamount case, the 8192^2 shelf-slope case "
-                        "(graph-replayed calls with varied ray counts) or the 8-scenario "
-                        "multi-source case")
+                   choices=["seamount", "planar_beach", "shelf_bump", "shelf_slope",
+                            "multi_source"],
+                   help="plain form: seamount (default), planar_beach, shelf_bump; batched "
+                        "form: seamount, the 8192^2 shelf-slope case (graph-replayed calls "
+                        "with varied ray counts) or the 8-scenario multi-source case")
     p.add_argument("--grid", type=int, default=None, help="grid points per axis override")
     p.add_argument("--no-autotune", action="store_true")
     return p.parse_args()
@@ -183,14 +184,35 @@ class ClockSampler:
                 "reasons": sorted(reasons)}
 
 
+PLAIN_WORKLOADS = ("seamount", "planar_beach", "shelf_bump")
+
+
+def plain_workload(args):
+    """The plain form's workload: the seamount case (default), the planar beach
+    (1,024 rays x 2,000 steps) or the shelf-bump differentiation field traced
+    forward (262,144 rays x 3,000 steps)."""
+    from mantaray_gb300 import workloads as W
+
+    if args.workload == "seamount":
+        return W.seamount(n_rays=args.rays, steps=args.trace_steps)
+    if args.workload == "planar_beach":
+        return W.planar_beach(n_rays=args.rays if args.rays != 65536 else 1024)
+    if args.workload == "shelf_bump":
+        return W.shelf_bump(n_rays=args.rays if args.rays != 65536 else 262144,
+                            steps=args.trace_steps if args.trace_steps != 4000 else 3000)
+    raise SystemExit(f"--workload {args.workload} runs in the batched form only")
+
+
+def grid_desc(w) -> str:
+    return f"{w.depth.shape[1]}x{w.depth.shape[0]} f64 depth/u/v"
+
+
 def reference_arm(args, rank: int, world: int):
     """The reference's CPU path (the oracle port: the Rust crate cannot be
     built here) on the host cores, each step a bounded sample."""
     if rank != 0:
         return
-    from mantaray_gb300.workloads import seamount
-
-    w = seamount(n_rays=args.rays, steps=args.trace_steps)
+    w = plain_workload(args)
     threads = cpu_threads()
     per_step = max(args.cpu_seconds / 4.0, 1.0)
     for _ in range(args.warmup):
@@ -207,7 +229,7 @@ def reference_arm(args, rank: int, world: int):
         "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "impl": "reference",
-        "config": {"workload": w.name, "rays": w.n, "grid": "2001x2001 f64", "dt": w.dt,
+        "config": {"workload": w.name, "rays": w.n, "grid": grid_desc(w), "dt": w.dt,
                    "parallelism": "host threads"},
         "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
                          "sample": descs[-1]},
@@ -220,7 +242,6 @@ def gb300_arm(args, rank: int, world: int, local_rank: int):
     import torch
 
     import mantaray_gb300 as mr
-    from mantaray_gb300.workloads import seamount
 
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
@@ -234,7 +255,7 @@ def gb300_arm(args, rank: int, world: int, local_rank: int):
         if dist is not None:
             dist.barrier()
 
-    w = seamount(n_rays=args.rays, steps=args.trace_steps)
+    w = plain_workload(args)
     b = mr.Bathymetry.grid(w.bx, w.by, w.depth)
     c = mr.Current.grid(w.cx, w.cy, w.u, w.v)
     rows = mr.num_steps(w.t0, w.t_end, w.dt) + 1
@@ -371,8 +392,12 @@ def gb300_arm(args, rank: int, world: int, local_rank: int):
                        "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"}
     # DRAM bytes of one full launch, scaled from the ncu capture of 16,384 rays
     # x 400 steps (221.9 MB) by ray-steps (profiles/rk4_f64_seamount_16384rays_400steps.md)
-    roofline["traffic"] = 221.9e6 * ray_steps / (16384 * 400)
-    roofline["traffic_note"] = "scaled from a 16,384-ray x 400-step ncu capture by ray-steps"
+    if args.workload == "seamount":
+        roofline["traffic"] = 221.9e6 * ray_steps / (16384 * 400)
+        roofline["traffic_note"] = "scaled from a 16,384-ray x 400-step ncu capture by ray-steps"
+    else:
+        roofline["traffic"] = None
+        roofline["flop_note"] = "flop_per_ray_step counted by ncu on the seamount workload"
     roofline["kernel_ms"] = 1e3 * kernel_s
 
     cpu = None
@@ -384,7 +409,7 @@ def gb300_arm(args, rank: int, world: int, local_rank: int):
         "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": w.name, "form": "plain FP64 (rk4_f64), one launch per call",
-                   "rays_per_gpu": n, "steps_per_ray": rows - 1, "grid": "2001x2001 f64 depth/u/v",
+                   "rays_per_gpu": n, "steps_per_ray": rows - 1, "grid": grid_desc(w),
                    "dt": w.dt, "stop_rule": "stage1", "math": args.math,
                    "other_math": {"math": alt_math, "value": alt_rate, "unit": METRIC},
                    "l2": "512 MB buffer written between timed steps; each step also writes 10.5 GB",
@@ -423,8 +448,8 @@ def batched_arm(args, rank: int, world: int, local_rank: int):
 
     graph_mode = False
     decimation = 0
-    if args.workload == "seamount":
-        w = W.seamount(n_rays=args.rays, steps=args.trace_steps)
+    if args.workload in PLAIN_WORKLOADS:
+        w = plain_workload(args)
         fields = [(w.bx, w.by, w.depth, w.cx, w.cy, w.u, w.v)]
         rays = {"x0": w.x0, "y0": w.y0, "kx0": w.kx0, "ky0": w.ky0, "scenario": None,
                 "t0": w.t0, "dt": w.dt, "steps": mr.num_steps(w.t0, w.t_end, w.dt)}
@@ -605,7 +630,7 @@ def batched_arm(args, rank: int, world: int, local_rank: int):
         roofline.update({"achieved": ach, "frac": ach / fp32_peak.value,
                          "flop_per_ray_step": FP32_FLOP_PER_RAY_STEP})
     cpu = None
-    if not args.no_cpu_baseline and args.workload == "seamount":
+    if not args.no_cpu_baseline and args.workload in PLAIN_WORKLOADS:
         cpu = cpu_baseline(w, args.cpu_seconds)
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,

@@ -10,6 +10,8 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <cmath>
+#include <cstring>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -188,6 +190,46 @@ int make_bathy_grid(size_t nx, size_t ny, const float *x, const float *y, const 
   return MR_OK;
 }
 
+// Cell thresholds of one current axis (fields.h): thr[j] = key of the smallest
+// double t with idx(t) >= j (j < n), thr[n] = key of the smallest t with
+// idx(t) > n - 1, where idx(t) = (t - a0) / sp exactly as
+// cartesian_current.rs:244-246 computes it.  idx is non-decreasing in t
+// (rounded subtraction and division by sp > 0 are monotone), so each
+// threshold is found by bisection over the ordered keys from -inf to +inf,
+// where idx(+inf) = +inf satisfies every predicate.
+std::vector<long long> current_axis_thresholds(double a0, double sp, size_t n) {
+  auto value = [](long long key) {
+    const long long bits = mr::order_key_bits(key);  // the key map is an involution
+    double t;
+    std::memcpy(&t, &bits, sizeof t);
+    return t;
+  };
+  auto key_of = [](double t) {
+    long long bits;
+    std::memcpy(&bits, &t, sizeof bits);
+    return mr::order_key_bits(bits);
+  };
+  const double high = static_cast<double>(n - 1);
+  std::vector<long long> thr(n + 1);
+  for (size_t j = 0; j <= n; ++j) {
+    const bool strict = j == n;
+    const double bound = strict ? high : static_cast<double>(j);
+    long long lo = key_of(-INFINITY), hi = key_of(INFINITY);
+    while (lo < hi) {
+      const long long mid =
+          lo + static_cast<long long>((static_cast<unsigned long long>(hi) -
+                                       static_cast<unsigned long long>(lo)) / 2);
+      const double idx = (value(mid) - a0) / sp;
+      if (strict ? idx > bound : idx >= bound)
+        hi = mid;
+      else
+        lo = mid + 1;
+    }
+    thr[j] = lo;
+  }
+  return thr;
+}
+
 int make_current_grid(size_t nx, size_t ny, const double *x, const double *y, const double *u,
                       size_t u_len, const double *v, size_t v_len, mr_current **out) {
   if (!out) return fail(MR_ERR_INVALID_ARGUMENT, "null output handle pointer");
@@ -217,6 +259,18 @@ int make_current_grid(size_t nx, size_t ny, const double *x, const double *y, co
     d.yspace = y[1] - y[0];
     d.inv_xsp = 1.0 / d.xsp;
     d.inv_ysp = 1.0 / d.ysp;
+  }
+  const bool use_thr = !h->one_point_axis && std::isfinite(d.x0) && std::isfinite(d.y0) &&
+                       std::isfinite(d.xsp) && std::isfinite(d.ysp) && d.xsp > 0.0 &&
+                       d.ysp > 0.0 && nx < (1u << 30) && ny < (1u << 30);
+  std::vector<long long> xthr, ythr;
+  if (use_thr) {
+    xthr = current_axis_thresholds(d.x0, d.xsp, nx);
+    ythr = current_axis_thresholds(d.y0, d.ysp, ny);
+    d.x0f = static_cast<float>(d.x0);
+    d.y0f = static_cast<float>(d.y0);
+    d.inv_xspf = static_cast<float>(d.inv_xsp);
+    d.inv_yspf = static_cast<float>(d.inv_ysp);
   }
   // Tables (fields.h): axes and values as f32 (interpolate, :375-396) and
   // the f64 cell gradients of :522-536.
@@ -251,7 +305,9 @@ int make_current_grid(size_t nx, size_t ny, const double *x, const double *y, co
       (e = upload(dudx.data(), len, &h->mem, &d.dudx)) != cudaSuccess ||
       (e = upload(dudy.data(), len, &h->mem, &d.dudy)) != cudaSuccess ||
       (e = upload(dvdx.data(), len, &h->mem, &d.dvdx)) != cudaSuccess ||
-      (e = upload(dvdy.data(), len, &h->mem, &d.dvdy)) != cudaSuccess) {
+      (e = upload(dvdy.data(), len, &h->mem, &d.dvdy)) != cudaSuccess ||
+      (use_thr && (e = upload(xthr.data(), nx + 1, &h->mem, &d.xthr)) != cudaSuccess) ||
+      (use_thr && (e = upload(ythr.data(), ny + 1, &h->mem, &d.ythr)) != cudaSuccess)) {
     free_mem(h->mem);
     delete h;
     return cuda_fail(e, "staging current grid");

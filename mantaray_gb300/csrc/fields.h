@@ -71,9 +71,27 @@ struct CurrentDev {
   double x0, xsp, xhigh;   // nearest() in f64
   double y0, ysp, yhigh;
   double inv_xsp, inv_ysp; // 1 / spacing (fast path of the index, lookup.cuh)
+  // Cell thresholds of each axis (lookup.cuh, corner_pair_thr): thr[j] is the
+  // order key (order_key below) of the smallest double t whose index
+  // (t - a0) / spacing, computed as the reference computes it, is >= j, for
+  // j = 0..n-1; thr[n] that of the smallest t whose index is > n - 1.  Null
+  // when an axis has fewer than two points or a spacing that is not finite
+  // and positive.
+  const long long *xthr, *ythr;
+  float x0f, inv_xspf;     // f32 first guess of the cell (any error is corrected)
+  float y0f, inv_yspf;
   double xspace, yspace;   // a[1] - a[0] (cartesian_current.rs:515-516)
   double cu, cv;           // constant current
 };
+
+// Key of a double under which signed integer order is the double order
+// (-0 just below +0; NaN outside -inf..+inf).
+#if defined(__CUDACC__)
+__host__ __device__
+#endif
+inline long long order_key_bits(long long bits) {
+  return bits ^ ((bits >> 63) & 0x7fffffffffffffffll);
+}
 
 // Error values of src/error.rs:7-37 that the right-hand side can produce.
 enum RhsError : int {

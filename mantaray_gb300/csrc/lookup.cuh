@@ -39,6 +39,26 @@ __device__ __forceinline__ double rceil(double v) { return ceil(v); }
 __device__ __forceinline__ float f32_nan() { return __int_as_float(0x7fffffff); }
 __device__ __forceinline__ double f64_nan() { return __longlong_as_double(0x7ff8000000000000ll); }
 
+// Exact f32 -> f64 conversion on the integer pipe for normal numbers and
+// zeros (re-biased exponent, mantissa shifted into place); subnormals,
+// infinities and NaN take the conversion instruction.  Same value as
+// static_cast<double>(f) in every case.
+__device__ __forceinline__ double f2d(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  if (e - 1u < 0xfeu)
+    return __hiloint2double(
+        static_cast<int>((u & 0x80000000u) | ((e + 896u) << 20) | ((u >> 3) & 0xfffffu)),
+        static_cast<int>(u << 29));
+  if ((u & 0x7fffffffu) == 0u) return __hiloint2double(static_cast<int>(u & 0x80000000u), 0);
+  return static_cast<double>(f);
+}
+
+// isnan for doubles on the integer pipe.
+__device__ __forceinline__ bool nan_bits(double v) {
+  return (__double_as_longlong(v) & 0x7fffffffffffffffll) > 0x7ff0000000000000ll;
+}
+
 // interpolator::bilinear, src/interpolator.rs:39-84.  Corners in the order
 // [(x1,y1), (x1,y2), (x2,y2), (x2,y1)] given as px/py/pv.
 __device__ __forceinline__ int bilinear_exact(const float px[4], const float py[4],
@@ -115,6 +135,43 @@ __device__ __forceinline__ int corner_pair_f64(double target, double a0, double 
     return RHS_OK;
   }
   return corner_pair<double>(target, a0, sp, high, lo, hi);
+}
+
+// The corner pair of corner_pair<double> from the axis thresholds of
+// fields.h, without FP64 arithmetic: with key = order_key(target),
+// idx(target) >= j exactly when key >= thr[j], so idx < 0 (key < thr[0]) and
+// idx > high (key >= thr[n]) are out of bounds, and otherwise the pair is
+// (i, i+1) for the i with thr[i] <= key < thr[i+1], except (high-1, high)
+// when idx == high -- the reference's edge, on-grid and interior rules
+// (cartesian_current.rs:283-339) all reduce to that.  An f32 estimate of idx
+// picks i; it is corrected by up to two cells (the estimate is within a
+// small fraction of a cell) and checked.  Returns RHS_OK or
+// RHS_INDEX_OUT_OF_BOUNDS, or -1 when the caller must use the exact rule
+// (NaN target, estimate not confirmed).
+__device__ __forceinline__ int corner_pair_thr(double target, float target32, float a0f,
+                                               float inv_spf, const long long *thr,
+                                               uint64_t n, uint64_t *lo, uint64_t *hi) {
+  const long long bits = __double_as_longlong(target);
+  if ((bits & 0x7fffffffffffffffll) > 0x7ff0000000000000ll) return -1;  // NaN
+  const long long key = order_key_bits(bits);
+  const int high = static_cast<int>(n) - 1;
+  if (key < __ldg(thr) || key >= __ldg(thr + n)) return RHS_INDEX_OUT_OF_BOUNDS;
+  float g = (target32 - a0f) * inv_spf;
+  g = fminf(fmaxf(g, 0.0f), static_cast<float>(high));  // NaN estimate -> 0
+  int i = __float2int_rz(g);
+  // thr[0] <= key < thr[n]: every step below stays inside 0..high.
+#pragma unroll
+  for (int it = 0; it < 2; ++it) {
+    if (key < __ldg(thr + i))
+      --i;
+    else if (key >= __ldg(thr + i + 1))
+      ++i;
+  }
+  if (key < __ldg(thr + i) || key >= __ldg(thr + i + 1)) return -1;
+  const int c = i < high ? i : high - 1;
+  *lo = static_cast<uint64_t>(c);
+  *hi = static_cast<uint64_t>(c) + 1;
+  return RHS_OK;
 }
 
 // BathymetryData::depth_and_gradient for every kind.  out = (h, dh/dx, dh/dy).
@@ -194,9 +251,14 @@ __device__ __forceinline__ int current_and_gradient(const CurrentDev &c, double 
   }
   // cartesian_current.rs:487-542
   uint64_t x1, x2, y1, y2;
-  int e = corner_pair_f64(x, c.x0, c.xsp, c.inv_xsp, c.xhigh, &x1, &x2);
+  const float tx = __double2float_rn(x), ty = __double2float_rn(y);
+  int e = -1;
+  if (c.xthr) e = corner_pair_thr(x, tx, c.x0f, c.inv_xspf, c.xthr, c.nx, &x1, &x2);
+  if (e < 0) e = corner_pair_f64(x, c.x0, c.xsp, c.inv_xsp, c.xhigh, &x1, &x2);
   if (e) return e;
-  e = corner_pair_f64(y, c.y0, c.ysp, c.inv_ysp, c.yhigh, &y1, &y2);
+  e = -1;
+  if (c.ythr) e = corner_pair_thr(y, ty, c.y0f, c.inv_yspf, c.ythr, c.ny, &y1, &y2);
+  if (e < 0) e = corner_pair_f64(y, c.y0, c.ysp, c.inv_ysp, c.yhigh, &y1, &y2);
   if (e) return e;
   const uint64_t sw = c.nx * y1 + x1, nw = c.nx * y2 + x1;
   const uint64_t ne = c.nx * y2 + x2, se = c.nx * y1 + x2;
@@ -206,14 +268,13 @@ __device__ __forceinline__ int current_and_gradient(const CurrentDev &c, double 
   const float ay1 = __ldg(c.y32 + y1), ay2 = __ldg(c.y32 + y2);
   const float px[4] = {ax1, ax1, ax2, ax2};
   const float py[4] = {ay1, ay2, ay2, ay1};
-  const float tx = __double2float_rn(x), ty = __double2float_rn(y);
   const float pu[4] = {__ldg(c.u32 + sw), __ldg(c.u32 + nw), __ldg(c.u32 + ne), __ldg(c.u32 + se)};
   const float pv[4] = {__ldg(c.v32 + sw), __ldg(c.v32 + nw), __ldg(c.v32 + ne), __ldg(c.v32 + se)};
   float u, v;
   if ((e = bilinear_exact(px, py, pu, tx, ty, &u))) return e;
   if ((e = bilinear_exact(px, py, pv, tx, ty, &v))) return e;
-  out[0] = static_cast<double>(u);
-  out[1] = static_cast<double>(v);
+  out[0] = f2d(u);
+  out[1] = f2d(v);
   if (x2 == x1 + 1 && y2 == y1 + 1) {
     out[2] = __ldg(c.dudx + sw);
     out[3] = __ldg(c.dudy + sw);

@@ -7,13 +7,18 @@
 //    within an ulp or two of glibc's);
 //  - RhsIdentity: the same quantities through exact identities that need
 //    fewer FP64 instructions -- cos(atan2(ky, kx)) = kx/k,
-//    sin(atan2(ky, kx)) = ky/k, and tanh, kh/cosh^2 and 1/(sinh cosh) of kh
-//    from the single value m = -expm1(-2kh) = 1 - exp(-2kh):
-//      tanh = m/(2-m),  kh/cosh^2 = 4 kh (1-m)/(2-m)^2,
-//      1/(sinh cosh) = 4 (1-m)/(m (2-m)),
-//    and sqrt(g k tanh) and 1/sqrt(g k tanh) from one rsqrt.  Each quantity
-//    differs from the libm form by a few ulps.
-// Compiled with -fmad=false (no contraction of the reference's arithmetic).
+//    sin(atan2(ky, kx)) = ky/k, and with a = kh, q = exp(-2a) from the single
+//    value m = -expm1(-2a) = 1 - q and w = 1/(m (1 + q)):
+//      tanh a = m / (1 + q),  a / cosh^2 a = 4 a q / (1 + q)^2,
+//      1 / (sinh a cosh a) = 4 q w,
+//    sqrt(g k tanh) and 1/sqrt(g k tanh) from one rsqrt, 1/k from another,
+//    and products and sums contracted into FMAs (kFma; the RK4 update too).
+//    Each quantity differs from the libm form by a few ulps.
+// Both read the field values through the exact lookups, convert f32 -> f64 on
+// the integer pipe (f2d) and test NaN / zero on bit patterns, which gives the
+// same values as the conversion and comparison instructions.
+// Compiled with -fmad=false: the reference's arithmetic is never contracted;
+// RhsIdentity's FMAs are explicit fma() calls.
 #pragma once
 
 #include <math.h>
@@ -25,6 +30,7 @@ namespace mr {
 constexpr double kG = 9.8;  // src/wave_ray_path.rs:23
 
 struct RhsLibm {
+  static constexpr bool kFma = false;
   // WaveRayPath::odes with group_velocity (:177-188) and dkdt_bathy
   // (:207-216) inlined in the reference's order.
   __device__ __forceinline__ static int odes(const BathyDev &b, const CurrentDev &c, double x,
@@ -32,9 +38,9 @@ struct RhsLibm {
     float hg[3];
     int e = depth_and_gradient(b, __double2float_rn(x), __double2float_rn(y), hg);
     if (e) return e;
-    const double h = static_cast<double>(hg[0]);
-    const double dhdx = static_cast<double>(hg[1]);
-    const double dhdy = static_cast<double>(hg[2]);
+    const double h = f2d(hg[0]);
+    const double dhdx = f2d(hg[1]);
+    const double dhdy = f2d(hg[2]);
     double cur[6];
     e = current_and_gradient(c, x, y, cur);
     if (e) return e;
@@ -63,36 +69,37 @@ struct RhsLibm {
 };
 
 struct RhsIdentity {
+  static constexpr bool kFma = true;
   __device__ __forceinline__ static int odes(const BathyDev &b, const CurrentDev &c, double x,
                                              double y, double kx, double ky, double out[4]) {
     float hg[3];
     int e = depth_and_gradient(b, __double2float_rn(x), __double2float_rn(y), hg);
     if (e) return e;
-    const double h = static_cast<double>(hg[0]);
     double cur[6];
     e = current_and_gradient(c, x, y, cur);
     if (e) return e;
-    const double k2 = kx * kx + ky * ky;
+    const double h = f2d(hg[0]);
+    const double k2 = fma(kx, kx, ky * ky);
     const double rk = rsqrt(k2);                    // 1/k
     const double k = k2 * rk;
-    if (!(h <= 0.0) && !(k > 0.0) && !isnan(k)) return RHS_ARGUMENT_OUT_OF_BOUNDS;
-    const double kh = k * h;
-    const double m = -expm1(-2.0 * kh);             // 1 - exp(-2kh)
-    const double q = 1.0 - m;                       // exp(-2kh)
-    const double inv_d = 1.0 / (m * (2.0 - m));     // one division for both below
-    const double r = m * inv_d;                     // 1 / (2 - m)
-    const double th = m * r;                        // tanh(kh)
-    const double kh_ch2 = 4.0 * kh * q * r * r;     // kh / cosh(kh)^2
-    const double inv_shch = 4.0 * q * (2.0 - m) * inv_d * r;  // 1 / (sinh cosh)
-    const double gkt = kG * k * th;
+    // group_velocity's k <= 0 error (h > 0 or NaN): k is >= 0 or NaN here
+    if (!(hg[0] <= 0.0f) && (__double_as_longlong(k) << 1) == 0) return RHS_ARGUMENT_OUT_OF_BOUNDS;
+    const double a = k * h;
+    const double m = -expm1(-2.0 * a);              // 1 - q
+    const double q = 1.0 - m;                       // exp(-2a)
+    const double w = __drcp_rn(m * (2.0 - m));      // 1 / (m (1 + q))
+    const double r = m * w;                         // 1 / (1 + q)
+    const double th = m * r;                        // tanh a
+    const double gkt = (kG * k) * th;
     const double rs = rsqrt(gkt);                   // 1 / sqrt(g k tanh)
-    double cg = (kG / 2.0) * (th + kh_ch2) * rs;
-    if (h <= 0.0) cg = f64_nan();
-    const double f = -0.5 * k * inv_shch * (gkt * rs);
-    out[0] = cg * (kx * rk) + cur[0];
-    out[1] = cg * (ky * rk) + cur[1];
-    out[2] = f * static_cast<double>(hg[1]) - kx * cur[2] - ky * cur[4];
-    out[3] = f * static_cast<double>(hg[2]) - kx * cur[3] - ky * cur[5];
+    const double q4 = 4.0 * q;
+    double cg = (kG / 2.0) * (fma(a * q4, r * r, th) * rs);
+    if (hg[0] <= 0.0f) cg = f64_nan();
+    const double f = (-0.5 * k) * ((q4 * w) * (gkt * rs));
+    out[0] = fma(cg, kx * rk, cur[0]);
+    out[1] = fma(cg, ky * rk, cur[1]);
+    out[2] = fma(f, f2d(hg[1]), -fma(kx, cur[2], ky * cur[4]));
+    out[3] = fma(f, f2d(hg[2]), -fma(kx, cur[3], ky * cur[5]));
     return RHS_OK;
   }
 };
@@ -107,7 +114,7 @@ __device__ __forceinline__ void system(const BathyDev &b, const CurrentDev &c, c
 }
 
 __device__ __forceinline__ bool all_nan4(const double v[4]) {
-  return isnan(v[0]) && isnan(v[1]) && isnan(v[2]) && isnan(v[3]);
+  return nan_bits(v[0]) && nan_bits(v[1]) && nan_bits(v[2]) && nan_bits(v[3]);
 }
 
 }  // namespace mr

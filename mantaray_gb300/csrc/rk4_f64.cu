@@ -11,8 +11,8 @@
 //
 // The right-hand side is a template parameter (RhsLibm: the reference's
 // transcendental calls; RhsIdentity: the same quantities from fewer FP64
-// instructions, see ray_exact.cuh).  Compiled with -fmad=false: no
-// contraction anywhere in this file.
+// instructions, see ray_exact.cuh).  Compiled with -fmad=false: nothing is
+// contracted implicitly; with RhsIdentity the RK4 update uses explicit FMAs.
 
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -43,6 +43,19 @@ __device__ __forceinline__ void store_nan_row(double *traj, uint64_t plane, uint
   for (int v = 0; v < 5; ++v) p[v * plane] = nan;
 }
 
+// Stage input y + k h, and the RK4 combination y + (k1 + 2 k2 + 2 k3 + k4) h/6:
+// the reference's operations (FMA = false) or the same sums as FMAs.
+template <bool FMA>
+__device__ __forceinline__ double stage_in(double y, double k, double h) {
+  return FMA ? fma(k, h, y) : y + k * h;
+}
+template <bool FMA>
+__device__ __forceinline__ double combine(double y, double k1, double k2, double k3, double k4,
+                                          double sixth) {
+  return FMA ? fma(fma(k3, 2.0, fma(k2, 2.0, k1)) + k4, sixth, y)
+             : y + (k1 + k2 * 2.0 + k3 * 2.0 + k4) * sixth;
+}
+
 template <int STOP_RULE, typename Rhs>
 __global__ void __launch_bounds__(kK1Block) rk4_f64_kernel(BathyDev b, CurrentDev c,
                                                            TraceArgs a) {
@@ -69,17 +82,17 @@ __global__ void __launch_bounds__(kK1Block) rk4_f64_kernel(BathyDev b, CurrentDe
     if (alive) {
       double k2[4], k3[4], k4[4], tmp[4];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) tmp[q] = y[q] + k1[q] * half;
+      for (int q = 0; q < 4; ++q) tmp[q] = stage_in<Rhs::kFma>(y[q], k1[q], half);
       system<Rhs>(b, c, tmp, k2);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) tmp[q] = y[q] + k2[q] * half;
+      for (int q = 0; q < 4; ++q) tmp[q] = stage_in<Rhs::kFma>(y[q], k2[q], half);
       system<Rhs>(b, c, tmp, k3);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) tmp[q] = y[q] + k3[q] * a.dt;
+      for (int q = 0; q < 4; ++q) tmp[q] = stage_in<Rhs::kFma>(y[q], k3[q], a.dt);
       system<Rhs>(b, c, tmp, k4);
       double yn[4];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) yn[q] = y[q] + (k1[q] + k2[q] * 2.0 + k3[q] * 2.0 + k4[q]) * sixth;
+      for (int q = 0; q < 4; ++q) yn[q] = combine<Rhs::kFma>(y[q], k1[q], k2[q], k3[q], k4[q], sixth);
       t = t + a.dt;
       store_row(a.traj, plane, a.n, s + 1, i, t, yn);
       ++rows;

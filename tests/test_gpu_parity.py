@@ -187,6 +187,40 @@ def test_current_gradient_grids(mr, oracle, fn):
     check(*r)
 
 
+def _around(v, k=3):
+    """v and its k nearest doubles on each side."""
+    out = [v]
+    lo = hi = v
+    for _ in range(k):
+        lo = np.nextafter(lo, -np.inf)
+        hi = np.nextafter(hi, np.inf)
+        out += [lo, hi]
+    return out
+
+
+def test_current_cells_at_grid_lines(mr, oracle):
+    # The current's cell index at and next to every grid line, on axes whose
+    # spacing is not a binary fraction, over a random current: a wrong cell
+    # changes the cell-constant gradients (cartesian_current.rs:515-536) and
+    # with them the first stage of the step.
+    rng = np.random.default_rng(31)
+    nx, ny = 48, 40
+    xs = 3.3 + 0.7 * np.arange(nx)
+    ys = -1.1 + 0.3 * np.arange(ny)
+    u = rng.normal(0.0, 0.3, (ny, nx))
+    v = rng.normal(0.0, 0.3, (ny, nx))
+    cur = ("grid", xs, ys, u, v)
+    px = np.array([t for a in xs for t in _around(float(a))] + [xs[0] - 0.01, xs[-1] + 0.01])
+    py = np.array([t for a in ys for t in _around(float(a))] + [ys[0] - 0.01, ys[-1] + 0.01])
+    x0 = np.concatenate([px, rng.uniform(xs[1], xs[-2], py.size)])
+    y0 = np.concatenate([rng.uniform(ys[1], ys[-2], px.size), py])
+    th = rng.uniform(0, 2 * np.pi, x0.size)
+    r = both(mr, oracle, ("constant", 50.0), cur, x0, y0, 0.05 * np.cos(th), 0.05 * np.sin(th),
+             0.0, 2.0, 0.5)
+    check(*r)
+    assert np.any(r[2] == 1) and np.any(r[1] > 2)
+
+
 def test_depth_len_shorter_than_grid(mr, oracle):
     # depth_at_indexes checks the flat index against the array length
     # (cartesian_netcdf3.rs:465-471): lookups past the end are errors (NaN).
