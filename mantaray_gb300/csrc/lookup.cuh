@@ -90,6 +90,59 @@ __device__ __forceinline__ int bilinear_exact(const float px[4], const float py[
   return RHS_OK;
 }
 
+// interpolator::bilinear for the corner quad the lookups build,
+// [(ax1,ay1), (ax1,ay2), (ax2,ay2), (ax2,ay1)], for NV value sets on the same
+// corners (depth; or u and v, which then share every step up to the
+// normalised coordinates, as they are the same operations on the same
+// inputs).  With finite corner coordinates and edges, bt0 = ax1 - ax1 and
+// dt1 = ay1 - ay1 are +0, so bt0*dt1 = +0, det = +0 - dt0*bt1, and the
+// diagonal of the inverse, +0/det, is +0 for det > 0 and -0 for det < 0
+// (det is never NaN there); everything else is the reference's operations in
+// its order (src/interpolator.rs:46-83).  Other quads take bilinear_exact.
+template <int NV>
+__device__ __forceinline__ int bilinear_cell(float ax1, float ax2, float ay1, float ay2,
+                                             const float (&pv)[NV][4], float tx, float ty,
+                                             float (&out)[NV]) {
+  const float px[4] = {ax1, ax1, ax2, ax2};
+  const float py[4] = {ay1, ay2, ay2, ay1};
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    if (tx == px[i] && ty == py[i]) {  // :46-50 coincident corner
+#pragma unroll
+      for (int v = 0; v < NV; ++v) out[v] = pv[v][i];
+      return RHS_OK;
+    }
+  }
+  const float bt1 = __fsub_rn(ay2, ay1);
+  const float dt0 = __fsub_rn(ax2, ax1);
+  if (!(isfinite(ax1) && isfinite(ay1) && isfinite(bt1) && isfinite(dt0))) {
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      const int e = bilinear_exact(px, py, pv[v], tx, ty, &out[v]);
+      if (e) return e;
+    }
+    return RHS_OK;
+  }
+  const float tt0 = __fsub_rn(tx, ax1), tt1 = __fsub_rn(ty, ay1);
+  const float det = __fsub_rn(0.0f, __fmul_rn(dt0, bt1));  // :64 with bt0*dt1 = +0
+  if (det == 0.0f) return RHS_INVALID_ARGUMENT;
+  const float m00 = det > 0.0f ? 0.0f : -0.0f;  // dt1 / det and bt0 / det
+  const float m01 = -__fdiv_rn(dt0, det);
+  const float m10 = -__fdiv_rn(bt1, det);
+  const float x = __fadd_rn(__fmul_rn(m00, tt0), __fmul_rn(m01, tt1));  // :74
+  const float y = __fadd_rn(__fmul_rn(m10, tt0), __fmul_rn(m00, tt1));  // :75
+#pragma unroll
+  for (int v = 0; v < NV; ++v) {
+    const float a00 = pv[v][0];
+    const float a10 = __fsub_rn(pv[v][1], pv[v][0]);
+    const float a01 = __fsub_rn(pv[v][3], pv[v][0]);
+    const float a11 = __fsub_rn(__fsub_rn(__fsub_rn(pv[v][2], pv[v][0]), a10), a01);
+    out[v] = __fadd_rn(__fadd_rn(__fadd_rn(a00, __fmul_rn(a10, x)), __fmul_rn(a01, y)),
+                       __fmul_rn(__fmul_rn(a11, x), y));  // :83, left to right
+  }
+  return RHS_OK;
+}
+
 // nearest + the edge/on-grid/interior corner rule (cartesian_netcdf3.rs:274-390
 // in f32, cartesian_current.rs:231-339 in f64).  a0/sp/high are the host
 // precomputed a[0], |a[1]-a[0]| and (n-1) as T; n >= 2.
@@ -190,19 +243,20 @@ __device__ __forceinline__ int depth_and_gradient(const BathyDev &b, float x, fl
     if (e) return e;
     // depth_at_indexes checks every corner's flat index against the array
     // length (:465-471); the largest of them is nx*y2 + x2.
-    const uint64_t sw = b.nx * y1 + x1, nw = b.nx * y2 + x1;
-    const uint64_t ne = b.nx * y2 + x2, se = b.nx * y1 + x2;
+    uint64_t sw, nw, ne, se;
+    if (x2 == x1 + 1 && y2 == y1 + 1) {
+      sw = b.nx * y1 + x1; nw = sw + b.nx; se = sw + 1; ne = nw + 1;
+    } else {
+      sw = b.nx * y1 + x1; nw = b.nx * y2 + x1; ne = b.nx * y2 + x2; se = b.nx * y1 + x2;
+    }
     if (ne >= b.depth_len) return RHS_INDEX_OUT_OF_BOUNDS;
-    const float ax1 = __ldg(b.x + x1), ax2 = __ldg(b.x + x2);
-    const float ay1 = __ldg(b.y + y1), ay2 = __ldg(b.y + y2);
-    const float px[4] = {ax1, ax1, ax2, ax2};
-    const float py[4] = {ay1, ay2, ay2, ay1};
-    const float pv[4] = {__ldg(b.depth32 + sw), __ldg(b.depth32 + nw), __ldg(b.depth32 + ne),
-                         __ldg(b.depth32 + se)};
-    float depth;
-    e = bilinear_exact(px, py, pv, x, y, &depth);
+    const float pv[1][4] = {{__ldg(b.depth32 + sw), __ldg(b.depth32 + nw),
+                             __ldg(b.depth32 + ne), __ldg(b.depth32 + se)}};
+    float depth[1];
+    e = bilinear_cell<1>(__ldg(b.x + x1), __ldg(b.x + x2), __ldg(b.y + y1), __ldg(b.y + y2), pv,
+                         x, y, depth);
     if (e) return e;
-    out[0] = depth;
+    out[0] = depth[0];
     if (x2 == x1 + 1 && y2 == y1 + 1) {
       out[1] = __ldg(b.gx + sw);
       out[2] = __ldg(b.gy + sw);
@@ -260,19 +314,22 @@ __device__ __forceinline__ int current_and_gradient(const CurrentDev &c, double 
   if (c.ythr) e = corner_pair_thr(y, ty, c.y0f, c.inv_yspf, c.ythr, c.ny, &y1, &y2);
   if (e < 0) e = corner_pair_f64(y, c.y0, c.ysp, c.inv_ysp, c.yhigh, &y1, &y2);
   if (e) return e;
-  const uint64_t sw = c.nx * y1 + x1, nw = c.nx * y2 + x1;
-  const uint64_t ne = c.nx * y2 + x2, se = c.nx * y1 + x2;
+  uint64_t sw, nw, ne, se;
+  if (x2 == x1 + 1 && y2 == y1 + 1) {
+    sw = c.nx * y1 + x1; nw = sw + c.nx; se = sw + 1; ne = nw + 1;
+  } else {
+    sw = c.nx * y1 + x1; nw = c.nx * y2 + x1; ne = c.nx * y2 + x2; se = c.nx * y1 + x2;
+  }
   // val_from_arr (:421-427) on u, then v: the largest flat index is ne.
   if (ne >= c.u_len || ne >= c.v_len) return RHS_INDEX_OUT_OF_BOUNDS;
-  const float ax1 = __ldg(c.x32 + x1), ax2 = __ldg(c.x32 + x2);
-  const float ay1 = __ldg(c.y32 + y1), ay2 = __ldg(c.y32 + y2);
-  const float px[4] = {ax1, ax1, ax2, ax2};
-  const float py[4] = {ay1, ay2, ay2, ay1};
-  const float pu[4] = {__ldg(c.u32 + sw), __ldg(c.u32 + nw), __ldg(c.u32 + ne), __ldg(c.u32 + se)};
-  const float pv[4] = {__ldg(c.v32 + sw), __ldg(c.v32 + nw), __ldg(c.v32 + ne), __ldg(c.v32 + se)};
-  float u, v;
-  if ((e = bilinear_exact(px, py, pu, tx, ty, &u))) return e;
-  if ((e = bilinear_exact(px, py, pv, tx, ty, &v))) return e;
+  const float pv[2][4] = {
+      {__ldg(c.u32 + sw), __ldg(c.u32 + nw), __ldg(c.u32 + ne), __ldg(c.u32 + se)},
+      {__ldg(c.v32 + sw), __ldg(c.v32 + nw), __ldg(c.v32 + ne), __ldg(c.v32 + se)}};
+  float uv[2];
+  if ((e = bilinear_cell<2>(__ldg(c.x32 + x1), __ldg(c.x32 + x2), __ldg(c.y32 + y1),
+                            __ldg(c.y32 + y2), pv, tx, ty, uv)))
+    return e;
+  const float u = uv[0], v = uv[1];
   out[0] = f2d(u);
   out[1] = f2d(v);
   if (x2 == x1 + 1 && y2 == y1 + 1) {

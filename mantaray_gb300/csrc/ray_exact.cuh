@@ -8,7 +8,7 @@
 //  - RhsIdentity: the same quantities through exact identities that need
 //    fewer FP64 instructions -- cos(atan2(ky, kx)) = kx/k,
 //    sin(atan2(ky, kx)) = ky/k, and with a = kh, q = exp(-2a) from the single
-//    value m = -expm1(-2a) = 1 - q and w = 1/(m (1 + q)):
+//    value m = -expm1(-2a) = 1 - q, and w = 1/(m (1 + q)):
 //      tanh a = m / (1 + q),  a / cosh^2 a = 4 a q / (1 + q)^2,
 //      1 / (sinh a cosh a) = 4 q w,
 //    sqrt(g k tanh) and 1/sqrt(g k tanh) from one rsqrt, 1/k from another,

@@ -43,22 +43,22 @@ __device__ __forceinline__ void store_nan_row(double *traj, uint64_t plane, uint
   for (int v = 0; v < 5; ++v) p[v * plane] = nan;
 }
 
-// Stage input y + k h, and the RK4 combination y + (k1 + 2 k2 + 2 k3 + k4) h/6:
-// the reference's operations (FMA = false) or the same sums as FMAs.
+// One RK4 step as four right-hand-side evaluations in a rolled loop (one copy
+// of the inlined right-hand side in the kernel, which keeps it in the
+// instruction cache): stages 0-2 evaluate at y + k h/2, y + k h/2, y + k h
+// and accumulate acc = k1 + k2*2 + k3*2 + k4 in the reference's left-to-right
+// order; stage 3 forms y' = y + acc * (h/6) and evaluates there, which is
+// the next step's first stage and the FRESH stop-rule derivative (system()
+// does not depend on t).  With FMA (RhsIdentity) the same sums are FMAs.
 template <bool FMA>
-__device__ __forceinline__ double stage_in(double y, double k, double h) {
+__device__ __forceinline__ double axpy(double y, double k, double h) {
   return FMA ? fma(k, h, y) : y + k * h;
-}
-template <bool FMA>
-__device__ __forceinline__ double combine(double y, double k1, double k2, double k3, double k4,
-                                          double sixth) {
-  return FMA ? fma(fma(k3, 2.0, fma(k2, 2.0, k1)) + k4, sixth, y)
-             : y + (k1 + k2 * 2.0 + k3 * 2.0 + k4) * sixth;
 }
 
 template <int STOP_RULE, typename Rhs>
 __global__ void __launch_bounds__(kK1Block) rk4_f64_kernel(BathyDev b, CurrentDev c,
                                                            TraceArgs a) {
+  constexpr bool F = Rhs::kFma;
   const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   const bool valid = i < a.n;
   const uint64_t plane = a.rows_cap * a.n;
@@ -80,30 +80,36 @@ __global__ void __launch_bounds__(kK1Block) rk4_f64_kernel(BathyDev b, CurrentDe
     // Once every lane of the warp has stopped, the rest is NaN padding.
     if (__all_sync(0xffffffffu, !alive)) break;
     if (alive) {
-      double k2[4], k3[4], k4[4], tmp[4];
+      double acc[4], kc[4], yn[4];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) tmp[q] = stage_in<Rhs::kFma>(y[q], k1[q], half);
-      system<Rhs>(b, c, tmp, k2);
+      for (int q = 0; q < 4; ++q) { acc[q] = k1[q]; kc[q] = k1[q]; }
+#pragma unroll 1
+      for (int st = 0; st < 4; ++st) {
+        double in[4];
+        if (st < 3) {
+          const double hs = st == 2 ? a.dt : half;
 #pragma unroll
-      for (int q = 0; q < 4; ++q) tmp[q] = stage_in<Rhs::kFma>(y[q], k2[q], half);
-      system<Rhs>(b, c, tmp, k3);
+          for (int q = 0; q < 4; ++q) in[q] = axpy<F>(y[q], kc[q], hs);
+        } else {
 #pragma unroll
-      for (int q = 0; q < 4; ++q) tmp[q] = stage_in<Rhs::kFma>(y[q], k3[q], a.dt);
-      system<Rhs>(b, c, tmp, k4);
-      double yn[4];
+          for (int q = 0; q < 4; ++q) { yn[q] = axpy<F>(y[q], acc[q], sixth); in[q] = yn[q]; }
+        }
+        system<Rhs>(b, c, in, kc);
+        if (st < 2) {
 #pragma unroll
-      for (int q = 0; q < 4; ++q) yn[q] = combine<Rhs::kFma>(y[q], k1[q], k2[q], k3[q], k4[q], sixth);
+          for (int q = 0; q < 4; ++q) acc[q] = axpy<F>(acc[q], kc[q], 2.0);
+        } else if (st == 2) {
+#pragma unroll
+          for (int q = 0; q < 4; ++q) acc[q] = acc[q] + kc[q];
+        }
+      }
       t = t + a.dt;
       store_row(a.traj, plane, a.n, s + 1, i, t, yn);
       ++rows;
-      // The next step's first stage doubles as the FRESH stop-rule derivative
-      // (system() does not depend on t).
-      double fresh[4];
-      system<Rhs>(b, c, yn, fresh);
-      const bool stop = STOP_RULE == 1 ? (all_nan4(fresh) || all_nan4(yn))
+      const bool stop = STOP_RULE == 1 ? (all_nan4(kc) || all_nan4(yn))
                                        : (all_nan4(k1) || all_nan4(yn));
 #pragma unroll
-      for (int q = 0; q < 4; ++q) { y[q] = yn[q]; k1[q] = fresh[q]; }
+      for (int q = 0; q < 4; ++q) { y[q] = yn[q]; k1[q] = kc[q]; }
       if (stop) alive = false;
     } else if (valid) {
       store_nan_row(a.traj, plane, a.n, s + 1, i);
