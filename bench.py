@@ -46,9 +46,9 @@ FP32_FLOP_PER_RAY_STEP = 541.7
 # DFMA = 2), per right-hand-side arithmetic, counted by ncu on the plain
 # kernel over the seamount workload
 # (sm__sass_thread_inst_executed_op_d{add,mul,fma}_pred_on; profiles/).
-FP64_FLOP_PER_RAY_STEP = {"libm": 1807.7, "identity": 339.0}
+FP64_FLOP_PER_RAY_STEP = {"libm": 1807.7, "identity": 340.6}
 # FP64-pipe instructions per ray-step (sm__inst_executed_pipe_fp64 x 32, same captures)
-FP64_PIPE_INST_PER_RAY_STEP = {"libm": 1218.4, "identity": 276.3}
+FP64_PIPE_INST_PER_RAY_STEP = {"libm": 1218.4, "identity": 288.7}
 
 
 def parse():
@@ -78,6 +78,9 @@ def parse():
                         "with varied ray counts) or the 8-scenario multi-source case")
     p.add_argument("--grid", type=int, default=None, help="grid points per axis override")
     p.add_argument("--no-autotune", action="store_true")
+    p.add_argument("--launch", default=None,
+                   help="batched form: fixed launch shape 'block,blocks_per_sm,rays_per_lane,"
+                        "order' instead of the autotuner's")
     return p.parse_args()
 
 
@@ -432,7 +435,7 @@ def batched_arm(args, rank: int, world: int, local_rank: int):
 
     import mantaray_gb300 as mr
     from mantaray_gb300 import workloads as W
-    from mantaray_gb300.batch import BatchTracer, default_config, endpoint_errors
+    from mantaray_gb300.batch import BatchTracer, default_config, endpoint_errors, make_config
 
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
@@ -481,7 +484,10 @@ def batched_arm(args, rank: int, world: int, local_rank: int):
 
     cfg = default_config()
     tuned = None
-    if not args.no_autotune:
+    if args.launch:
+        blk, bps, rpl, order = (int(v) for v in args.launch.split(","))
+        cfg = make_config(blk, bps, rpl, 32, order)
+    elif not args.no_autotune:
         probe = min(n_all, 1 << 20)
         pin = [t[:probe] for t in ins]
         cfg = tracer.autotune(*pin, dt, min(steps, 200), t0=t0,
@@ -576,11 +582,11 @@ def batched_arm(args, rank: int, world: int, local_rank: int):
         return
 
     # ---- the plain FP64 form on a subset of the same rays, and the error ----
-    # plain FP64 rate on a GPU-filling subset; errors on up to 4,096 of its rays
-    sub = int(min(n_all, 65536 if steps <= 4000 else 16384))
+    # plain FP64 rate on a GPU-filling subset (one stream per scenario, all
+    # launched together); errors on up to 4,096 of its rays
+    sub = int(min(n_all, 65536))
     idx = np.sort(rng.choice(n_all, sub, replace=False))
     scen_of = rays["scenario"][idx] if rays["scenario"] is not None else np.zeros(sub, np.uint8)
-    plain_steps, plain_time = 0, 0.0
     errs_all = {"rel_position": [], "direction": [], "compared": 0, "n": 0}
     ref_out = tracer.trace(*[t[torch.from_numpy(idx).to(dev)] for t in ins], dt, steps, t0=t0,
                            scenario=(torch.from_numpy(scen_of).to(dev)
@@ -588,6 +594,8 @@ def batched_arm(args, rank: int, world: int, local_rank: int):
     torch.cuda.synchronize()
     end_sub = ref_out.end_state.cpu().numpy()
     nst_sub = ref_out.n_steps.cpu().numpy()
+    del ref_out
+    launches_plain = []
     for s_i, (b, c) in enumerate(handles):
         m = np.nonzero(scen_of == s_i)[0]
         if m.size == 0:
@@ -598,14 +606,22 @@ def batched_arm(args, rank: int, world: int, local_rank: int):
         traj = torch.empty((5, steps + 1, sel.size), dtype=torch.float64, device=dev)
         nr = torch.empty(sel.size, dtype=torch.int32, device=dev)
         st = torch.empty(sel.size, dtype=torch.uint8, device=dev)
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
+        launches_plain.append((s_i, m, b, c, pin, traj, nr, st, torch.cuda.Stream(dev)))
+    torch.cuda.synchronize()
+    e_start = torch.cuda.Event(enable_timing=True)
+    e_start.record(stream)
+    ends = []
+    for s_i, m, b, c, pin, traj, nr, st, strm in launches_plain:
+        strm.wait_event(e_start)
         mr.trace_device(b, c, *pin, t0, t0 + steps * dt, dt, traj, nr, st, math="identity",
-                        stream=stream)
-        e1.record(stream)
-        e1.synchronize()
-        plain_time += e0.elapsed_time(e1) / 1e3
+                        stream=strm)
+        e = torch.cuda.Event(enable_timing=True)
+        e.record(strm)
+        ends.append(e)
+    torch.cuda.synchronize()
+    plain_time = max(e_start.elapsed_time(e) for e in ends) / 1e3
+    plain_steps = 0
+    for s_i, m, b, c, pin, traj, nr, st, strm in launches_plain:
         plain_steps += int((nr.to(torch.int64) - 1).sum().item())
         k = min(m.size, max(1, 4096 // len(handles)))
         er = endpoint_errors(end_sub[:, m[:k]], nst_sub[m[:k]], traj[:, :, :k].cpu().numpy(),
@@ -614,7 +630,7 @@ def batched_arm(args, rank: int, world: int, local_rank: int):
         errs_all["direction"].append(er["direction"])
         errs_all["compared"] += er["compared"]
         errs_all["n"] += er["n"]
-        del traj
+    del launches_plain
     rel = np.concatenate(errs_all["rel_position"])
     dth = np.concatenate(errs_all["direction"])
     plain_rate = plain_steps / plain_time

@@ -200,6 +200,9 @@ typedef struct mr_batch_config {
   int blocks_per_sm;   /* resident blocks per SM of the persistent grid */
   int rays_per_lane;   /* 1 or 2 rays interleaved per thread */
   int rebase_interval; /* steps between FP64 origin rebases */
+  int order;           /* 1: sort the rays by starting cell and direction before
+                          tracing, so a warp's rays share cell records (results
+                          per ray are unchanged); 0: trace in index order */
 } mr_batch_config;
 
 /* Per-ray status of the batched form. */

@@ -32,8 +32,9 @@ def default_config() -> N.BatchConfig:
     return cfg
 
 
-def make_config(block=128, blocks_per_sm=4, rays_per_lane=1, rebase_interval=32) -> N.BatchConfig:
-    return N.BatchConfig(block, blocks_per_sm, rays_per_lane, rebase_interval)
+def make_config(block=128, blocks_per_sm=4, rays_per_lane=1, rebase_interval=32,
+                order=0) -> N.BatchConfig:
+    return N.BatchConfig(block, blocks_per_sm, rays_per_lane, rebase_interval, order)
 
 
 @dataclass
@@ -126,8 +127,9 @@ class BatchTracer:
                 _TUNE_CACHE[key] = stored[key]
                 return make_config(**stored[key])
         if candidates is None:
-            candidates = [make_config(b, bps, rpl, 32)
-                          for b, bps, rpl in itertools.product((64, 128, 256), (2, 4, 8), (1, 2))
+            candidates = [make_config(b, bps, rpl, 32, order)
+                          for b, bps, rpl, order in itertools.product((64, 128, 256), (2, 4, 8),
+                                                                      (1, 2), (0, 1))
                           if b * bps <= 2048]
         out = self.alloc(int(x0.numel()), probe_steps, 0, device=x0.device)
         best, best_t = None, float("inf")

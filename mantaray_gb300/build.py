@@ -36,6 +36,7 @@ UNITS = {
     "batch_api.cu": [],
     "batch_static.cu": [],
     "diff.cu": [],
+    "order.cu": [],
 }
 
 

@@ -60,6 +60,24 @@ struct BatchArgs {
   int32_t *n_saved;          // [n] rows stored in `saved`
   uint8_t *status;           // [n] BatchStatus
   unsigned long long *queue; // work-queue head (scratch, zeroed before the launch)
+  const uint32_t *order;     // [n] ray taken at each queue slot, or null (slot = ray)
+};
+
+// Spatial ordering of the rays (order.cu): keys [2][n_max] and values
+// [2][n_max] ping-pong buffers, per-tile digit counts [256][tiles].
+constexpr int kOrderTile = 4096;
+struct OrderArgs {
+  const ScenarioDev *scen;
+  int n_scenarios;
+  const uint8_t *ray_scenario;
+  const double *x0, *y0, *kx0, *ky0;
+  int64_t n;                 // rays of this call (<= the capacity the grids are sized for)
+  int64_t *n_dev;            // device copy of n for the kernels after order_keys
+  uint64_t *keys[2];
+  uint32_t *vals[2];
+  uint32_t *counts;
+  int tiles;                 // ceil(capacity / kOrderTile)
+  int scen_shift;            // bit position of the scenario in the key
 };
 
 }  // namespace mr

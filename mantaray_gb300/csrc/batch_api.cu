@@ -5,6 +5,7 @@
 #include <math.h>
 #include <string.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "../../include/mantaray_gpu.h"
@@ -18,9 +19,13 @@ struct mr_batch_graph {
   mr_batch *batch = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
-  cudaGraphNode_t kernel_node = nullptr;
+  cudaGraphNode_t kernel_node = nullptr;   // the batched kernel
   cudaKernelNodeParams params{};
   mr::BatchArgs args{};
+  cudaGraphNode_t order_node = nullptr;    // order_keys, when the rays are ordered
+  cudaKernelNodeParams order_params{};
+  mr::OrderArgs oargs{};
+  mr_order_buffers ord;                    // the graph's own ordering scratch
   size_t n_max = 0;
 };
 
@@ -88,6 +93,51 @@ int pack_current(mr_batch *b, const mr_current *c, mr::PackedGrid *g, cudaStream
   return MR_OK;
 }
 
+void order_free(mr_order_buffers *o) {
+  if (o->mem) cudaFree(o->mem);
+  *o = mr_order_buffers();
+}
+
+// Makes the ordering scratch hold at least n rays (the old contents are not
+// kept; cudaFree waits for work that still uses them).
+cudaError_t order_reserve(mr_order_buffers *o, size_t n) {
+  if (n <= o->cap && o->mem) return cudaSuccess;
+  order_free(o);
+  const int tiles = mr::order_tiles(static_cast<int64_t>(n));
+  auto up = [](size_t v) { return (v + 255) & ~static_cast<size_t>(255); };
+  const size_t keys = up(n * sizeof(uint64_t)), vals = up(n * sizeof(uint32_t));
+  const size_t counts = up(256ull * tiles * sizeof(uint32_t));
+  char *p = nullptr;
+  cudaError_t e = cudaMalloc(reinterpret_cast<void **>(&p), 256 + 2 * keys + 2 * vals + counts);
+  if (e != cudaSuccess) return e;
+  o->mem = p;
+  o->cap = n;
+  o->tiles = tiles;
+  o->n_dev = reinterpret_cast<int64_t *>(p);
+  o->keys[0] = reinterpret_cast<uint64_t *>(p + 256);
+  o->keys[1] = reinterpret_cast<uint64_t *>(p + 256 + keys);
+  o->vals[0] = reinterpret_cast<uint32_t *>(p + 256 + 2 * keys);
+  o->vals[1] = reinterpret_cast<uint32_t *>(p + 256 + 2 * keys + vals);
+  o->counts = reinterpret_cast<uint32_t *>(p + 256 + 2 * keys + 2 * vals);
+  return cudaSuccess;
+}
+
+mr::OrderArgs order_args(const mr_batch *b, const mr::BatchArgs &a, const mr_order_buffers &o) {
+  mr::OrderArgs r{};
+  r.scen = a.scen;
+  r.n_scenarios = a.n_scenarios;
+  r.ray_scenario = a.ray_scenario;
+  r.x0 = a.x0; r.y0 = a.y0; r.kx0 = a.kx0; r.ky0 = a.ky0;
+  r.n = a.n;
+  r.n_dev = o.n_dev;
+  r.keys[0] = o.keys[0]; r.keys[1] = o.keys[1];
+  r.vals[0] = o.vals[0]; r.vals[1] = o.vals[1];
+  r.counts = o.counts;
+  r.tiles = o.tiles;
+  r.scen_shift = b->order_scen_shift;
+  return r;
+}
+
 int check_config(const mr_batch_config *cfg) {
   if (!cfg) return fail(MR_ERR_INVALID_ARGUMENT, "null config");
   if (cfg->block < 32 || cfg->block > 256 || cfg->block % 32)
@@ -98,6 +148,8 @@ int check_config(const mr_batch_config *cfg) {
     return fail(MR_ERR_INVALID_ARGUMENT, "rays_per_lane must be 1 or 2");
   if (cfg->rebase_interval < 1)
     return fail(MR_ERR_INVALID_ARGUMENT, "rebase_interval must be >= 1");
+  if (cfg->order != 0 && cfg->order != 1)
+    return fail(MR_ERR_INVALID_ARGUMENT, "order must be 0 or 1");
   return MR_OK;
 }
 
@@ -143,13 +195,22 @@ int fill_args(mr_batch *b, size_t n, size_t n_stride, const uint8_t *ray_scenari
 }
 
 // Stream work of one batched call: reset the queue, NaN-fill the saved rows
-// (rows a ray does not reach stay NaN, as the reference pads them), launch.
-cudaError_t enqueue(const mr::BatchArgs &a, const mr_batch_config *cfg, cudaStream_t s) {
+// (rows a ray does not reach stay NaN, as the reference pads them), order
+// the rays when cfg->order (into `ord`, sized for n_stride rays), launch.
+cudaError_t enqueue(const mr_batch *b, mr::BatchArgs a, const mr_batch_config *cfg,
+                    const mr_order_buffers *ord, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(a.queue, 0, sizeof(unsigned long long), s);
   if (e != cudaSuccess) return e;
   if (a.decimation > 0 && a.save_cap > 0) {
     e = cudaMemsetAsync(a.saved, 0xFF, sizeof(float) * 5 * a.save_cap * a.n_stride, s);
     if (e != cudaSuccess) return e;
+  }
+  a.order = nullptr;
+  if (cfg->order) {
+    const mr::OrderArgs o = order_args(b, a, *ord);
+    e = mr::launch_order(o, a.n_stride, b->order_passes, s);
+    if (e != cudaSuccess) return e;
+    a.order = ord->vals[b->order_passes & 1];
   }
   return mr::launch_rk4_f32(a, cfg->block, cfg->blocks_per_sm, cfg->rays_per_lane, s);
 }
@@ -164,6 +225,7 @@ int mr_batch_default_config(mr_batch_config *cfg) {
   cfg->blocks_per_sm = 4;
   cfg->rays_per_lane = 1;
   cfg->rebase_interval = 32;
+  cfg->order = 0;
   return MR_OK;
 }
 
@@ -197,6 +259,19 @@ int mr_batch_create(size_t n_scenarios, const mr_bathymetry *const *bathy,
                         cudaMemcpyHostToDevice, s);
   if (rc == MR_OK && e == cudaSuccess)
     e = cudaMalloc(reinterpret_cast<void **>(&b->queue), sizeof(unsigned long long));
+  if (rc == MR_OK) {
+    // ordering key: direction in bits 0-7, the Morton code of the starting
+    // cell (cbits per axis) above it, the scenario above that
+    int cmax = 1;
+    for (const auto &sc : b->host_scen)
+      cmax = std::max(cmax, std::max(sc.bathy.nx - 1, sc.bathy.ny - 1));
+    int cbits = 0;
+    while (cbits < 16 && (1 << cbits) < cmax) ++cbits;
+    int sbits = 0;
+    while ((1 << sbits) < b->n_scenarios) ++sbits;
+    b->order_scen_shift = 8 + 2 * cbits;
+    b->order_passes = (b->order_scen_shift + sbits + 7) / 8;
+  }
   if (rc == MR_OK && e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (rc == MR_OK && e != cudaSuccess) rc = cuda_fail(e, "building the batched scenarios");
   if (rc != MR_OK) {
@@ -213,6 +288,7 @@ void mr_batch_destroy(mr_batch *b) {
   for (void *p : b->mem) cudaFree(p);
   if (b->scen) cudaFree(b->scen);
   if (b->queue) cudaFree(b->queue);
+  order_free(&b->ord);
   delete b;
 }
 
@@ -229,7 +305,14 @@ int mr_batch_trace_device(mr_batch *b, size_t n, const uint8_t *ray_scenario, co
   DeviceGuard g(b->device);
   if (!g.ok()) return fail(MR_ERR_CUDA, "cannot select the batch's device");
   cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : cudaStreamPerThread;
-  cudaError_t e = enqueue(a, cfg, s);
+  cudaError_t e = cudaSuccess;
+  if (cfg->order) {
+    // the scratch may be in use by earlier calls on this stream: order them first
+    if (n > b->ord.cap) e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = order_reserve(&b->ord, n);
+    if (e != cudaSuccess) return cuda_fail(e, "ordering scratch");
+  }
+  e = enqueue(b, a, cfg, &b->ord, s);
   if (e != cudaSuccess) return cuda_fail(e, "rk4_f32 launch");
   return MR_OK;
 }
@@ -253,10 +336,15 @@ int mr_batch_graph_create(mr_batch *b, size_t n_max, const uint8_t *ray_scenario
   gr->args = a;
   gr->n_max = n_max;
   cudaStream_t s = nullptr;
-  cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  cudaError_t e = cudaSuccess;
+  if (cfg->order) {
+    e = order_reserve(&gr->ord, n_max);
+    gr->oargs = order_args(b, a, gr->ord);
+  }
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
-    cudaError_t le = enqueue(a, cfg, s);
+    cudaError_t le = enqueue(b, a, cfg, &gr->ord, s);
     e = cudaStreamEndCapture(s, &gr->graph);
     if (le != cudaSuccess) e = le;
   }
@@ -269,10 +357,19 @@ int mr_batch_graph_create(mr_batch *b, size_t n_max, const uint8_t *ray_scenario
     cudaGraphNodeType type;
     e = cudaGraphNodeGetType(nodes[i], &type);
     if (e == cudaSuccess && type == cudaGraphNodeTypeKernel) {
-      gr->kernel_node = nodes[i];
-      e = cudaGraphKernelNodeGetParams(nodes[i], &gr->params);
+      cudaKernelNodeParams p{};
+      e = cudaGraphKernelNodeGetParams(nodes[i], &p);
+      if (e != cudaSuccess) break;
+      if (p.func == mr::order_keys_function()) {
+        gr->order_node = nodes[i];
+        gr->order_params = p;
+      } else if (p.func == mr::rk4_f32_function(cfg->rays_per_lane)) {
+        gr->kernel_node = nodes[i];
+        gr->params = p;
+      }
     }
   }
+  if (e == cudaSuccess && cfg->order && !gr->order_node) e = cudaErrorInvalidValue;
   if (s) cudaStreamDestroy(s);
   if (e == cudaSuccess && !gr->kernel_node) e = cudaErrorInvalidValue;
   if (e != cudaSuccess) {
@@ -296,6 +393,14 @@ int mr_batch_graph_launch(mr_batch_graph *gr, size_t n, void *stream) {
   p.kernelParams = kargs;
   p.extra = nullptr;
   cudaError_t e = cudaGraphExecKernelNodeSetParams(gr->exec, gr->kernel_node, &p);
+  if (e == cudaSuccess && gr->order_node) {
+    gr->oargs.n = static_cast<int64_t>(n);
+    void *oargs[1] = {&gr->oargs};
+    cudaKernelNodeParams q = gr->order_params;
+    q.kernelParams = oargs;
+    q.extra = nullptr;
+    e = cudaGraphExecKernelNodeSetParams(gr->exec, gr->order_node, &q);
+  }
   if (e == cudaSuccess)
     e = cudaGraphLaunch(gr->exec, stream ? static_cast<cudaStream_t>(stream) : cudaStreamPerThread);
   if (e != cudaSuccess) return cuda_fail(e, "launching the batched graph");
@@ -307,6 +412,7 @@ void mr_batch_graph_destroy(mr_batch_graph *gr) {
   DeviceGuard g(gr->batch ? gr->batch->device : 0);
   if (gr->exec) cudaGraphExecDestroy(gr->exec);
   if (gr->graph) cudaGraphDestroy(gr->graph);
+  order_free(&gr->ord);
   delete gr;
 }
 

@@ -1,9 +1,24 @@
 // batch_handle.h -- the mr_batch handle (internal).
 #pragma once
 
+#include <stdint.h>
+
 #include <vector>
 
 #include "batch.h"
+
+// Device scratch of the spatial ordering (order.cu) for up to `cap` rays:
+// one allocation holding n_dev, keys [2][cap], vals [2][cap], counts
+// [256][tiles].
+struct mr_order_buffers {
+  void *mem = nullptr;
+  size_t cap = 0;
+  int tiles = 0;
+  int64_t *n_dev = nullptr;
+  uint64_t *keys[2] = {nullptr, nullptr};
+  uint32_t *vals[2] = {nullptr, nullptr};
+  uint32_t *counts = nullptr;
+};
 
 struct mr_batch {
   int device = 0;
@@ -12,4 +27,7 @@ struct mr_batch {
   mr::ScenarioDev *scen = nullptr;   // device copy of host_scen
   std::vector<void *> mem;           // packed cells
   unsigned long long *queue = nullptr;  // work-queue head (device scratch)
+  mr_order_buffers ord;              // ordering scratch of direct calls, grown on demand
+  int order_scen_shift = 8;          // key layout of the ordering (order.cu)
+  int order_passes = 1;
 };

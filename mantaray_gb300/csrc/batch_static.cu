@@ -82,6 +82,9 @@ extern "C" int mr_batch_trace_device_static(
       cfg->blocks_per_sm > 32 || (cfg->rays_per_lane != 1 && cfg->rays_per_lane != 2) ||
       cfg->rebase_interval < 1)
     return fail(MR_ERR_INVALID_ARGUMENT, "bad launch configuration");
+  if (cfg->order != 0)
+    return fail(MR_ERR_INVALID_ARGUMENT,
+                "ray ordering needs scratch memory; use mr_batch_trace_device");
   if (n > 0 && (!x0 || !y0 || !kx0 || !ky0 || !end_state || !n_steps || !n_saved || !status))
     return fail(MR_ERR_INVALID_ARGUMENT, "null array argument");
   if (decimation < 0 || max_steps < 0 || max_steps >= INT32_MAX)

@@ -33,5 +33,13 @@ cudaError_t launch_pack_bathy(const BathyDev &b, float4 *cells, cudaStream_t str
 cudaError_t launch_pack_current(const CurrentDev &c, float4 *cells, cudaStream_t stream);
 cudaError_t launch_rk4_f32(const BatchArgs &a, int block, int blocks_per_sm, int rays_per_lane,
                            cudaStream_t stream);
+const void *rk4_f32_function(int rays_per_lane);
+
+// Spatial ordering of a batched call's rays (K6): sorts by key in `passes`
+// 8-bit digits; the order is then o.vals[passes & 1].  Grids are sized for
+// n_max >= o.n.
+int order_tiles(int64_t n_max);
+cudaError_t launch_order(const OrderArgs &o, int64_t n_max, int passes, cudaStream_t stream);
+const void *order_keys_function();
 
 }  // namespace mr

@@ -308,7 +308,7 @@ __global__ void __launch_bounds__(256) rk4_f32_kernel(BatchArgs a) {
         base = __shfl_sync(kFull, base, leader);
         if (L[j].ray == -1) {
           const int64_t r = static_cast<int64_t>(base) + __popc(need & lt_mask);
-          if (r < n) start(a, L[j], r);
+          if (r < n) start(a, L[j], a.order ? static_cast<int64_t>(__ldg(a.order + r)) : r);
           else L[j].ray = -2;
         }
       }
@@ -359,6 +359,11 @@ cudaError_t launch_rk4_f32(const BatchArgs &a, int block, int blocks_per_sm, int
   else
     rk4_f32_kernel<1><<<grid, block, 0, stream>>>(a);
   return cudaGetLastError();
+}
+
+const void *rk4_f32_function(int rays_per_lane) {
+  return rays_per_lane == 2 ? reinterpret_cast<const void *>(&rk4_f32_kernel<2>)
+                            : reinterpret_cast<const void *>(&rk4_f32_kernel<1>);
 }
 
 }  // namespace mr

@@ -123,8 +123,10 @@ def test_launch_shapes_give_identical_results(mr):
     tracer = BatchTracer([(b, c)])
     x0, y0, kx0, ky0 = _dev(w.x0, w.y0, w.kx0, w.ky0)
     ref = None
+    # ordered configurations take the rays in another order: same results
     for cfg in (make_config(128, 4, 1, 32), make_config(64, 8, 2, 32), make_config(256, 2, 1, 32),
-                make_config(32, 1, 2, 32)):
+                make_config(32, 1, 2, 32), make_config(128, 4, 1, 32, 1),
+                make_config(64, 2, 2, 32, 1)):
         res = tracer.trace(x0, y0, kx0, ky0, w.dt, 500, decimation=50, config=cfg)
         got = [t.cpu().numpy() for t in (res.end_state, res.n_steps, res.status, res.saved)]
         if ref is None:
@@ -134,9 +136,10 @@ def test_launch_shapes_give_identical_results(mr):
                 np.testing.assert_array_equal(np.nan_to_num(a, nan=-7.0), np.nan_to_num(b_, nan=-7.0))
 
 
-def test_multiple_scenarios(mr, oracle):
+@pytest.mark.parametrize("order", [0, 1])
+def test_multiple_scenarios(mr, oracle, order):
     # three scenarios with different fields; each ray must see its own
-    from mantaray_gb300.batch import BatchTracer, endpoint_errors
+    from mantaray_gb300.batch import BatchTracer, endpoint_errors, make_config
 
     rng = np.random.default_rng(21)
     scen = []
@@ -158,7 +161,8 @@ def test_multiple_scenarios(mr, oracle):
     tracer = BatchTracer(fields)
     dx0, dy0, dkx, dky = _dev(x0, y0, kx0, ky0)
     (dsid,) = _dev(sid)
-    res = tracer.trace(dx0, dy0, dkx, dky, 1.0, 600, scenario=dsid)
+    res = tracer.trace(dx0, dy0, dkx, dky, 1.0, 600, scenario=dsid,
+                       config=make_config(128, 4, 1, 32, order))
     end = res.end_state.cpu().numpy()
     nst = res.n_steps.cpu().numpy()
     for s in range(3):
@@ -170,10 +174,11 @@ def test_multiple_scenarios(mr, oracle):
         check_errors(errs, f"scenario {s}")
 
 
-def test_graph_replay_matches_direct_calls(mr):
+@pytest.mark.parametrize("order", [0, 1])
+def test_graph_replay_matches_direct_calls(mr, order):
     import torch
 
-    from mantaray_gb300.batch import BatchTracer
+    from mantaray_gb300.batch import BatchTracer, make_config
     from mantaray_gb300.workloads import seamount
 
     w = seamount(n_rays=8192, steps=300)
@@ -182,7 +187,8 @@ def test_graph_replay_matches_direct_calls(mr):
     x0, y0, kx0, ky0 = _dev(w.x0, w.y0, w.kx0, w.ky0)
     direct = tracer.trace(x0, y0, kx0, ky0, w.dt, 300, decimation=30)
     d_end = direct.end_state.cpu().numpy()
-    g = tracer.graph(x0, y0, kx0, ky0, w.dt, 300, decimation=30)
+    g = tracer.graph(x0, y0, kx0, ky0, w.dt, 300, decimation=30,
+                     config=make_config(128, 4, 1, 32, order))
     for n in (8192, 4096, 6000, 8192):
         g.out.n_steps.fill_(-1)
         g.launch(n)
