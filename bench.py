@@ -490,7 +490,7 @@ def batched_arm(args, rank: int, world: int, local_rank: int):
     elif not args.no_autotune:
         probe = min(n_all, 1 << 20)
         pin = [t[:probe] for t in ins]
-        cfg = tracer.autotune(*pin, dt, min(steps, 200), t0=t0,
+        cfg = tracer.autotune(*pin, dt, min(steps, 1000), t0=t0,
                               scenario=sid[:probe] if sid is not None else None,
                               cache_key=f"{torch.cuda.get_device_name(dev)}:{name}:{probe}")
         tuned = cfg.as_dict()

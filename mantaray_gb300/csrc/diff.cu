@@ -416,6 +416,11 @@ __global__ void __launch_bounds__(64) diff_tangent_kernel(DiffArgs<T> A) {
   A.status[i] = ok ? 0 : 1;
 }
 
+// FP64 keeps the four stages' partials per backward step; FP32 re-evaluates
+// them (its right-hand side is cheap and the registers bound its occupancy).
+template <typename T>
+constexpr bool kStorePoints = sizeof(T) == 8;
+
 template <typename T>
 __global__ void __launch_bounds__(64) diff_adjoint_kernel(DiffArgs<T> A) {
   const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -449,31 +454,64 @@ __global__ void __launch_bounds__(64) diff_adjoint_kernel(DiffArgs<T> A) {
     for (int64_t s = last - 1; s >= first; --s) {
 #pragma unroll
       for (int q = 0; q < 4; ++q) y[q] = A.seg[((s - first) * 4 + q) * A.n + i];
-      Point<T> P1, P2, P3, P4;
       T k1[4], k2[4], k3[4], k4[4], Y2[4], Y3[4], Y4[4];
-      eval(A, y, P1, k1);
-#pragma unroll
-      for (int q = 0; q < 4; ++q) Y2[q] = y[q] + k1[q] * half;
-      eval(A, Y2, P2, k2);
-#pragma unroll
-      for (int q = 0; q < 4; ++q) Y3[q] = y[q] + k2[q] * half;
-      eval(A, Y3, P3, k3);
-#pragma unroll
-      for (int q = 0; q < 4; ++q) Y4[q] = y[q] + k3[q] * h;
-      eval(A, Y4, P4, k4);
       T w[4], r4[4], r3[4], r2[4], r1[4];
+      if (kStorePoints<T>) {
+        // keep the four stages' partials (registers are traded for
+        // right-hand-side evaluations where those are expensive: FP64)
+        Point<T> P1, P2, P3, P4;
+        eval(A, y, P1, k1);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) w[q] = lam[q] * (h / T(6));
-      vjp(A, Y4, P4, w, r4, acc);
+        for (int q = 0; q < 4; ++q) Y2[q] = y[q] + k1[q] * half;
+        eval(A, Y2, P2, k2);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) w[q] = lam[q] * (h / T(3)) + h * r4[q];
-      vjp(A, Y3, P3, w, r3, acc);
+        for (int q = 0; q < 4; ++q) Y3[q] = y[q] + k2[q] * half;
+        eval(A, Y3, P3, k3);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) w[q] = lam[q] * (h / T(3)) + half * r3[q];
-      vjp(A, Y2, P2, w, r2, acc);
+        for (int q = 0; q < 4; ++q) Y4[q] = y[q] + k3[q] * h;
+        eval(A, Y4, P4, k4);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) w[q] = lam[q] * (h / T(6)) + half * r2[q];
-      vjp(A, y, P1, w, r1, acc);
+        for (int q = 0; q < 4; ++q) w[q] = lam[q] * (h / T(6));
+        vjp(A, Y4, P4, w, r4, acc);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) w[q] = lam[q] * (h / T(3)) + h * r4[q];
+        vjp(A, Y3, P3, w, r3, acc);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) w[q] = lam[q] * (h / T(3)) + half * r3[q];
+        vjp(A, Y2, P2, w, r2, acc);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) w[q] = lam[q] * (h / T(6)) + half * r2[q];
+        vjp(A, y, P1, w, r1, acc);
+      } else {
+        // keep only the stage states and evaluate each stage again when its
+        // transpose is applied: one live Point, far fewer registers
+        Point<T> P;
+        eval(A, y, P, k1);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) Y2[q] = y[q] + k1[q] * half;
+        eval(A, Y2, P, k2);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) Y3[q] = y[q] + k2[q] * half;
+        eval(A, Y3, P, k3);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) Y4[q] = y[q] + k3[q] * h;
+        eval(A, Y4, P, k4);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) w[q] = lam[q] * (h / T(6));
+        vjp(A, Y4, P, w, r4, acc);
+        eval(A, Y3, P, k3);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) w[q] = lam[q] * (h / T(3)) + h * r4[q];
+        vjp(A, Y3, P, w, r3, acc);
+        eval(A, Y2, P, k2);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) w[q] = lam[q] * (h / T(3)) + half * r3[q];
+        vjp(A, Y2, P, w, r2, acc);
+        eval(A, y, P, k1);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) w[q] = lam[q] * (h / T(6)) + half * r2[q];
+        vjp(A, y, P, w, r1, acc);
+      }
 #pragma unroll
       for (int q = 0; q < 4; ++q) lam[q] = lam[q] + r1[q] + r2[q] + r3[q] + r4[q];
     }
