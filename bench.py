@@ -31,6 +31,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
+from mantaray_gb300.distributed import reduce_scalar  # noqa: E402
+
 METRIC = "ray-steps/s"
 L2_FLUSH_BYTES = 512 << 20  # > 129 MB L2
 
@@ -299,11 +301,7 @@ def gb300_arm(args, rank: int, world: int, local_rank: int):
     clock = clocks.summary()
     ray_steps = int(torch.sum(n_rows.to(torch.int64) - 1).item())
     local_t = sum(times)
-    t_max = local_t
-    if dist is not None:
-        tt = torch.tensor([local_t], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_max = float(tt.item())
+    t_max = reduce_scalar(local_t, "max") if dist is not None else local_t
     total_ray_steps = ray_steps * args.steps * world
     value = total_ray_steps / t_max
     kernel_s = local_t / args.steps
@@ -342,11 +340,7 @@ def gb300_arm(args, rank: int, world: int, local_rank: int):
             e2e_times.append(time.perf_counter() - t0)
         barrier()
         e2e_local = sum(e2e_times)
-        e2e_max = e2e_local
-        if dist is not None:
-            tt = torch.tensor([e2e_local], device=dev)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            e2e_max = float(tt.item())
+        e2e_max = reduce_scalar(e2e_local, "max") if dist is not None else e2e_local
         e2e_steps = int(np.sum(res.n_rows.astype(np.int64) - 1))
         e2e = {"value": e2e_steps * args.steps * world / e2e_max, "unit": METRIC,
                "h2d_bytes_per_step": 4 * n * 8,
@@ -536,11 +530,7 @@ def batched_arm(args, rank: int, world: int, local_rank: int):
         barrier()
     clock = clocks.summary()
     local_t = sum(times)
-    t_max = local_t
-    if dist is not None:
-        tt = torch.tensor([local_t], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_max = float(tt.item())
+    t_max = reduce_scalar(local_t, "max") if dist is not None else local_t
     value = done_steps * world / t_max
     kernel_rate = done_steps / local_t
 
@@ -588,6 +578,7 @@ def batched_arm(args, rank: int, world: int, local_rank: int):
     idx = np.sort(rng.choice(n_all, sub, replace=False))
     scen_of = rays["scenario"][idx] if rays["scenario"] is not None else np.zeros(sub, np.uint8)
     errs_all = {"rel_position": [], "direction": [], "compared": 0, "n": 0}
+    sens = []
     ref_out = tracer.trace(*[t[torch.from_numpy(idx).to(dev)] for t in ins], dt, steps, t0=t0,
                            scenario=(torch.from_numpy(scen_of).to(dev)
                                      if rays["scenario"] is not None else None), config=cfg)
@@ -630,9 +621,25 @@ def batched_arm(args, rank: int, world: int, local_rank: int):
         errs_all["direction"].append(er["direction"])
         errs_all["compared"] += er["compared"]
         errs_all["n"] += er["n"]
+        # the FP64 model's own sensitivity: the same rays started 1 cm further in x
+        pin_p = [pin[0][:k] + 0.01, pin[1][:k], pin[2][:k], pin[3][:k]]
+        traj_p = torch.empty((5, steps + 1, k), dtype=torch.float64, device=dev)
+        nr_p = torch.empty(k, dtype=torch.int32, device=dev)
+        st_p = torch.empty(k, dtype=torch.uint8, device=dev)
+        mr.trace_device(b, c, *pin_p, t0, t0 + steps * dt, dt, traj_p, nr_p, st_p,
+                        math="identity", stream=stream)
+        tp, np_ = traj_p.cpu().numpy(), nr_p.cpu().numpy().astype(np.int64)
+        ik = np.arange(k)
+        last = np_ - 1
+        last = np.where(np.all(np.isfinite(tp[1:, last, ik]), axis=0), last, np.maximum(last - 1, 0))
+        es = endpoint_errors(tp[:, last, ik], last, traj[:, :, :k].cpu().numpy(),
+                             nr[:k].cpu().numpy())
+        sens.append(es["rel_position"])
+        del traj_p
     del launches_plain
     rel = np.concatenate(errs_all["rel_position"])
     dth = np.concatenate(errs_all["direction"])
+    sens_all = np.concatenate(sens)
     plain_rate = plain_steps / plain_time
 
     L = mr._native.load()
@@ -666,6 +673,10 @@ def batched_arm(args, rank: int, world: int, local_rank: int):
                        "rel_position_max": float(rel.max()),
                        "direction_p99_rad": float(np.percentile(dth, 99)),
                        "direction_max_rad": float(dth.max())},
+                   "fp64_endpoint_change_for_1cm_start_shift": {
+                       "rel_position_p50": float(np.median(sens_all)),
+                       "rel_position_p99": float(np.percentile(sens_all, 99)),
+                       "rel_position_max": float(sens_all.max())},
                    "l2": "512 MB buffer written between timed steps",
                    "parallelism": f"replicas x{world}"},
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
