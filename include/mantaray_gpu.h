@@ -318,6 +318,33 @@ int mr_diff_tangent(int precision, const mr_diff_grid *bgrid, const void *depth,
                     const void *d_u, const void *d_v, double dt, int64_t steps,
                     void *end_state, void *d_end, uint8_t *status, void *stream);
 
+/* ---- initial states on the device -------------------------------------------
+ * The reference's notebooks build initial states on the host: a launch point
+ * or a start line, directions, and |k| from the period by the dispersion
+ * relation (notebooks/canonical_examples/utils.py:11-26,
+ * notebooks/agulhas/notebook/src.py:60-82).  These write them straight into
+ * device arrays for the batched form.  Ray r gets direction
+ * theta0 + (theta1 - theta0) * u and period period0 + (period1 - period0) * v
+ * with u, v in [0, 1) from SplitMix64 of (seed, r) (u evenly spaced,
+ * (j + 0.5) / count, with MR_SEED_EVEN_DIRECTIONS); |k| solves
+ * (2 pi / T)^2 = g k tanh(k h), g = 9.8, by Newton iteration in FP64 at the
+ * depth h the bathymetry handle's lookup gives at the launch point (NaN
+ * states where there is none).  Device arrays; asynchronous on `stream`. */
+#define MR_SEED_EVEN_DIRECTIONS 0x1
+
+/* n_sources points (sx, sy: device arrays), rays_per_source rays each, ray
+ * r = s * rays_per_source + j; outputs [n_sources * rays_per_source]. */
+int mr_seed_point_sources(const mr_bathymetry *b, size_t n_sources, const double *sx,
+                          const double *sy, size_t rays_per_source, double theta0,
+                          double theta1, double period0, double period1, uint64_t seed,
+                          int flags, double *x0, double *y0, double *kx0, double *ky0,
+                          void *stream);
+
+/* n rays evenly spaced from (xa, ya) to (xb, yb) (numpy.linspace points). */
+int mr_seed_line(const mr_bathymetry *b, double xa, double ya, double xb, double yb, size_t n,
+                 double theta0, double theta1, double period0, double period1, uint64_t seed,
+                 int flags, double *x0, double *y0, double *kx0, double *ky0, void *stream);
+
 /* ---- NetCDF-3 access (host only, no GPU) ---------------------------------- */
 
 /* Reads variable `name` of a NetCDF-3 file converted to f64 (the reference's

@@ -37,7 +37,10 @@ SYMBOLS = (
     "mr_batch_default_config", "mr_batch_create", "mr_batch_destroy", "mr_batch_trace_device",
     "mr_batch_graph_create", "mr_batch_graph_launch", "mr_batch_graph_destroy",
     "mr_batch_trace_device_static", "mr_diff_forward", "mr_diff_backward", "mr_diff_tangent",
+    "mr_seed_point_sources", "mr_seed_line",
 )
+
+SEED_EVEN_DIRECTIONS = 0x1
 
 BATCH_STATIC_MAX_SCENARIOS = 64
 
@@ -140,6 +143,10 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
                                                ctypes.c_int64, ctypes.c_int64, sz, vp, vp, vp,
                                                vp, vp, P(BatchConfig), vp]),
         "mr_batch_graph_destroy": (None, [vp]),
+        "mr_seed_point_sources": (i32, [vp, sz, vp, vp, sz, f64, f64, f64, f64, ctypes.c_uint64,
+                                        i32, vp, vp, vp, vp, vp]),
+        "mr_seed_line": (i32, [vp, f64, f64, f64, f64, sz, f64, f64, f64, f64, ctypes.c_uint64,
+                               i32, vp, vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

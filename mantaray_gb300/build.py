@@ -37,6 +37,7 @@ UNITS = {
     "batch_static.cu": [],
     "diff.cu": [],
     "order.cu": [],
+    "seed.cu": ["-fmad=false"],
 }
 
 

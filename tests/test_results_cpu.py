@@ -62,3 +62,4 @@ def test_trace_result_methods(tmp_path):
     p = tmp_path / "rays.tsv"
     res.append_tsv(p, 1)
     assert p.read_text() == "t x y kx ky\n0 3 1 0.25 0  \n1 4 1 0.25 0  \nEND\n"
+
