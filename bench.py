@@ -46,11 +46,11 @@ OUT_BYTES_PER_ROW = 5 * 8
 FP32_FLOP_PER_RAY_STEP = 541.7
 # FP64 floating-point operations one ray-step executes (DADD/DMUL = 1,
 # DFMA = 2), per right-hand-side arithmetic, counted by ncu on the plain
-# kernel over the seamount workload
+# kernel over the seamount workload (65,536 rays x 100 steps)
 # (sm__sass_thread_inst_executed_op_d{add,mul,fma}_pred_on; profiles/).
-FP64_FLOP_PER_RAY_STEP = {"libm": 1807.7, "identity": 340.6}
+FP64_FLOP_PER_RAY_STEP = {"libm": 1818.1, "identity": 340.6}
 # FP64-pipe instructions per ray-step (sm__inst_executed_pipe_fp64 x 32, same captures)
-FP64_PIPE_INST_PER_RAY_STEP = {"libm": 1218.4, "identity": 288.7}
+FP64_PIPE_INST_PER_RAY_STEP = {"libm": 1226.0, "identity": 288.7}
 
 
 def parse():
@@ -387,11 +387,11 @@ def gb300_arm(args, rank: int, world: int, local_rank: int):
                        "frac": hbm_achieved / hbm_peak,
                        "bytes_per_ray_step": GRID_BYTES_PER_RAY_STEP + OUT_BYTES_PER_ROW,
                        "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"}
-    # DRAM bytes of one full launch, scaled from the ncu capture of 16,384 rays
-    # x 400 steps (221.9 MB) by ray-steps (profiles/rk4_f64_seamount_16384rays_400steps.md)
+    # DRAM bytes of one full launch, scaled from the ncu capture of 65,536 rays
+    # x 100 steps (217.04 MB) by ray-steps (profiles/rk4_f64_seamount_65536rays_100steps.md)
     if args.workload == "seamount":
-        roofline["traffic"] = 221.9e6 * ray_steps / (16384 * 400)
-        roofline["traffic_note"] = "scaled from a 16,384-ray x 400-step ncu capture by ray-steps"
+        roofline["traffic"] = 217.04e6 * ray_steps / (65536 * 100)
+        roofline["traffic_note"] = "scaled from a 65,536-ray x 100-step ncu capture by ray-steps"
     else:
         roofline["traffic"] = None
         roofline["flop_note"] = "flop_per_ray_step counted by ncu on the seamount workload"

@@ -146,6 +146,8 @@ struct RayLane {
   float cpx, cpy, ckx, cky;  // Kahan compensations
   int64_t step;
   int32_t saved;
+  int32_t to_save;    // steps until the next decimated row (no 64-bit modulo per step)
+  int32_t to_rebase;  // steps until the next origin rebase
 };
 
 // Right-hand side in FP32 at offset (px, py); returns a BatchStatus.
@@ -235,6 +237,12 @@ __device__ __forceinline__ void finish(const BatchArgs &a, RayLane &L, int statu
   L.ray = -1;
 }
 
+// The decimation as a step countdown (a ray takes fewer than 2^31 steps, so
+// a larger decimation saves no row after step 0 either way).
+__device__ __forceinline__ int32_t save_period(const BatchArgs &a) {
+  return a.decimation > 0x7fffffff ? 0x7fffffff : static_cast<int32_t>(a.decimation);
+}
+
 __device__ __forceinline__ void start(const BatchArgs &a, RayLane &L, int64_t r) {
   L.ray = r;
   L.scen = a.ray_scenario ? static_cast<int>(a.ray_scenario[r]) : 0;
@@ -249,6 +257,8 @@ __device__ __forceinline__ void start(const BatchArgs &a, RayLane &L, int64_t r)
   L.pc = grid_pos(s.current, L.ox, L.oy);
   L.step = 0;
   L.saved = 0;
+  L.to_save = save_period(a);
+  L.to_rebase = a.rebase_interval;
   if (a.decimation > 0) {
     save_row(a, L);
     L.saved = 1;
@@ -280,11 +290,15 @@ __device__ __forceinline__ int advance(const BatchArgs &a, RayLane &L) {
   kahan_add(L.kx, L.ckx, k1[2]);
   kahan_add(L.ky, L.cky, k1[3]);
   ++L.step;
-  if (a.decimation > 0 && L.step % a.decimation == 0) {
+  if (a.decimation > 0 && --L.to_save == 0) {
+    L.to_save = save_period(a);
     save_row(a, L);
     ++L.saved;
   }
-  if (L.step % a.rebase_interval == 0) rebase(s, L);
+  if (--L.to_rebase == 0) {
+    L.to_rebase = a.rebase_interval;
+    rebase(s, L);
+  }
   return BATCH_COMPLETE;
 }
 
