@@ -653,8 +653,21 @@ def batched_arm(args, rank: int, world: int, local_rank: int):
         roofline.update({"achieved": ach, "frac": ach / fp32_peak.value,
                          "flop_per_ray_step": FP32_FLOP_PER_RAY_STEP})
     cpu = None
-    if not args.no_cpu_baseline and args.workload in PLAIN_WORKLOADS:
-        cpu = cpu_baseline(w, args.cpu_seconds)
+    if not args.no_cpu_baseline:
+        if args.workload in PLAIN_WORKLOADS:
+            cpu = cpu_baseline(w, args.cpu_seconds)
+        else:
+            # the first scenario's fields with a seeded sample of its rays
+            f = fields[0]
+            pick = np.nonzero(rays["scenario"] == 0)[0] if rays["scenario"] is not None \
+                else np.arange(n_all)
+            pick = np.sort(np.random.default_rng(11).choice(pick, min(pick.size, 65536),
+                                                           replace=False))
+            wc = W.Workload(name + "_scenario0_sample", *f, *(rays[k][pick] for k in
+                                                              ("x0", "y0", "kx0", "ky0")),
+                            t0, t0 + steps * dt, dt)
+            cpu = cpu_baseline(wc, args.cpu_seconds)
+            cpu["sample"] += "; scenario 0's fields, a seeded 65,536-ray sample of its rays"
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
