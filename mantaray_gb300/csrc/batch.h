@@ -25,6 +25,7 @@ struct PackedGrid {
   double x0, y0;         // first axis values
   double sp_x, sp_y;     // axis spacing (a[1] - a[0])
   float inv_sp_x, inv_sp_y;
+  double inv_sp_xd, inv_sp_yd;  // 1 / spacing in FP64 (origin rebase)
   int kind;              // 0 grid, 1 constant (current only)
   float cu, cv;          // constant current
 };

@@ -100,7 +100,7 @@ struct GridPos {
 
 __device__ __forceinline__ GridPos grid_pos(const PackedGrid &g, double ox, double oy) {
   GridPos p;
-  const double ux = (ox - g.x0) / g.sp_x, uy = (oy - g.y0) / g.sp_y;
+  const double ux = (ox - g.x0) * g.inv_sp_xd, uy = (oy - g.y0) * g.inv_sp_yd;
   const double fx = floor(ux), fy = floor(uy);
   // clamp far-away origins so the int conversion stays defined; such a lane
   // fails the in-range test of its first lookup
