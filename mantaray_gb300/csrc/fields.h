@@ -19,6 +19,8 @@
 
 #include <stdint.h>
 
+#include "bits.h"
+
 namespace mr {
 
 enum BathyKind : int {
@@ -83,15 +85,6 @@ struct CurrentDev {
   double xspace, yspace;   // a[1] - a[0] (cartesian_current.rs:515-516)
   double cu, cv;           // constant current
 };
-
-// Key of a double under which signed integer order is the double order
-// (-0 just below +0; NaN outside -inf..+inf).
-#if defined(__CUDACC__)
-__host__ __device__
-#endif
-inline long long order_key_bits(long long bits) {
-  return bits ^ ((bits >> 63) & 0x7fffffffffffffffll);
-}
 
 // Error values of src/error.rs:7-37 that the right-hand side can produce.
 enum RhsError : int {

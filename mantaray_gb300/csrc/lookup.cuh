@@ -39,26 +39,6 @@ __device__ __forceinline__ double rceil(double v) { return ceil(v); }
 __device__ __forceinline__ float f32_nan() { return __int_as_float(0x7fffffff); }
 __device__ __forceinline__ double f64_nan() { return __longlong_as_double(0x7ff8000000000000ll); }
 
-// Exact f32 -> f64 conversion on the integer pipe for normal numbers and
-// zeros (re-biased exponent, mantissa shifted into place); subnormals,
-// infinities and NaN take the conversion instruction.  Same value as
-// static_cast<double>(f) in every case.
-__device__ __forceinline__ double f2d(float f) {
-  const unsigned u = __float_as_uint(f);
-  const unsigned e = (u >> 23) & 0xffu;
-  if (e - 1u < 0xfeu)
-    return __hiloint2double(
-        static_cast<int>((u & 0x80000000u) | ((e + 896u) << 20) | ((u >> 3) & 0xfffffu)),
-        static_cast<int>(u << 29));
-  if ((u & 0x7fffffffu) == 0u) return __hiloint2double(static_cast<int>(u & 0x80000000u), 0);
-  return static_cast<double>(f);
-}
-
-// isnan for doubles on the integer pipe.
-__device__ __forceinline__ bool nan_bits(double v) {
-  return (__double_as_longlong(v) & 0x7fffffffffffffffll) > 0x7ff0000000000000ll;
-}
-
 // interpolator::bilinear, src/interpolator.rs:39-84.  Corners in the order
 // [(x1,y1), (x1,y2), (x2,y2), (x2,y1)] given as px/py/pv.
 __device__ __forceinline__ int bilinear_exact(const float px[4], const float py[4],
@@ -305,7 +285,7 @@ __device__ __forceinline__ int current_and_gradient(const CurrentDev &c, double 
   }
   // cartesian_current.rs:487-542
   uint64_t x1, x2, y1, y2;
-  const float tx = __double2float_rn(x), ty = __double2float_rn(y);
+  const float tx = d2f(x), ty = d2f(y);
   int e = -1;
   if (c.xthr) e = corner_pair_thr(x, tx, c.x0f, c.inv_xspf, c.xthr, c.nx, &x1, &x2);
   if (e < 0) e = corner_pair_f64(x, c.x0, c.xsp, c.inv_xsp, c.xhigh, &x1, &x2);

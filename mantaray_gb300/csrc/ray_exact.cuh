@@ -14,9 +14,9 @@
 //    sqrt(g k tanh) and 1/sqrt(g k tanh) from one rsqrt, 1/k from another,
 //    and products and sums contracted into FMAs (kFma; the RK4 update too).
 //    Each quantity differs from the libm form by a few ulps.
-// Both read the field values through the exact lookups, convert f32 -> f64 on
-// the integer pipe (f2d) and test NaN / zero on bit patterns, which gives the
-// same values as the conversion and comparison instructions.
+// Both read the field values through the exact lookups, convert between f32
+// and f64 on the integer pipe (bits.h) and test NaN / zero on bit patterns,
+// which gives the same values as the conversion and comparison instructions.
 // Compiled with -fmad=false: the reference's arithmetic is never contracted;
 // RhsIdentity's FMAs are explicit fma() calls.
 #pragma once
@@ -36,7 +36,7 @@ struct RhsLibm {
   __device__ __forceinline__ static int odes(const BathyDev &b, const CurrentDev &c, double x,
                                              double y, double kx, double ky, double out[4]) {
     float hg[3];
-    int e = depth_and_gradient(b, __double2float_rn(x), __double2float_rn(y), hg);
+    int e = depth_and_gradient(b, d2f(x), d2f(y), hg);
     if (e) return e;
     const double h = f2d(hg[0]);
     const double dhdx = f2d(hg[1]);
@@ -73,7 +73,7 @@ struct RhsIdentity {
   __device__ __forceinline__ static int odes(const BathyDev &b, const CurrentDev &c, double x,
                                              double y, double kx, double ky, double out[4]) {
     float hg[3];
-    int e = depth_and_gradient(b, __double2float_rn(x), __double2float_rn(y), hg);
+    int e = depth_and_gradient(b, d2f(x), d2f(y), hg);
     if (e) return e;
     double cur[6];
     e = current_and_gradient(c, x, y, cur);
