@@ -44,6 +44,14 @@ OUT_BYTES_PER_ROW = 5 * 8
 # FP32 floating-point operations one ray-step of the batched kernel executes
 # (FADD/FMUL = 1, FFMA = 2), counted by ncu on the seamount workload.
 FP32_FLOP_PER_RAY_STEP = 541.7
+# Algorithmic work of one ray-step (the reference's arithmetic, hand count from
+# src/wave_ray_path.rs:118-216 plus the RK4 update): ~55 FP64 add/mul/div per
+# right-hand side x 4 + ~53 for the update = 270 (36 transcendental calls not
+# counted); its f32 interpolation adds ~440 FP32 operations (4 stages x 3
+# bilinears of ~35 operations, plus index arithmetic).  The batched form does
+# all of it in FP32: 710.
+ALG_FP64_FLOP_PER_RAY_STEP = 270.0
+ALG_FP32_FLOP_PER_RAY_STEP = 710.0
 # FP64 floating-point operations one ray-step executes (DADD/DMUL = 1,
 # DFMA = 2), per right-hand-side arithmetic, counted by ncu on the plain
 # kernel over the seamount workload (65,536 rays x 100 steps)
@@ -369,20 +377,23 @@ def gb300_arm(args, rank: int, world: int, local_rank: int):
     except (OSError, ValueError):
         pass
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    flop_per_rs = FP64_FLOP_PER_RAY_STEP.get(args.math)
-    if flop_per_rs:
-        fp64_achieved = rs_per_s_kernel * flop_per_rs / 1e12
-        roofline = {"bound": "fp64", "achieved": fp64_achieved, "peak": fp64_peak.value,
-                    "unit": "TFLOP/s", "frac": fp64_achieved / fp64_peak.value,
-                    "peak_source": "measured: FP64 FMA-chain kernel on this GPU, this run",
-                    "flop_per_ray_step": flop_per_rs,
-                    "pipe_issue_frac": rs_per_s_kernel * FP64_PIPE_INST_PER_RAY_STEP[args.math]
-                    / (fp64_peak.value * 1e12 / 2.0),
-                    "pipe_issue_note": "FP64-pipe instructions/s over the FMA-chain DFMA/s"}
-    else:
-        roofline = {"bound": "fp64", "achieved": None, "peak": fp64_peak.value,
-                    "unit": "TFLOP/s", "frac": None,
-                    "peak_source": "measured: FP64 FMA-chain kernel on this GPU, this run"}
+    # achieved = the algorithmic FP64 work of a ray-step (ALG_FP64_FLOP_PER_RAY_STEP)
+    # x ray-steps per second of the kernel; the executed work (ncu) beside it
+    fp64_achieved = rs_per_s_kernel * ALG_FP64_FLOP_PER_RAY_STEP / 1e12
+    exec_flop = FP64_FLOP_PER_RAY_STEP[args.math]
+    roofline = {"bound": "fp64", "achieved": fp64_achieved, "peak": fp64_peak.value,
+                "unit": "TFLOP/s", "frac": fp64_achieved / fp64_peak.value,
+                "peak_source": "measured: FP64 FMA-chain kernel on this GPU, this run",
+                "flop_per_ray_step": ALG_FP64_FLOP_PER_RAY_STEP,
+                "flop_note": "algorithmic: 4 x ~55 RHS + ~53 RK4-update FP64 add/mul/div per "
+                             "ray-step (the reference's expressions); its 36 transcendental "
+                             "calls are not counted",
+                "executed_flop_per_ray_step": exec_flop,
+                "executed_frac": rs_per_s_kernel * exec_flop / 1e12 / fp64_peak.value,
+                "pipe_issue_frac": rs_per_s_kernel * FP64_PIPE_INST_PER_RAY_STEP[args.math]
+                / (fp64_peak.value * 1e12 / 2.0),
+                "pipe_issue_note": "FP64-pipe instructions/s (ncu count per ray-step) over the "
+                                   "FMA-chain DFMA/s"}
     roofline["hbm"] = {"achieved": hbm_achieved, "peak": hbm_peak, "unit": "GB/s",
                        "frac": hbm_achieved / hbm_peak,
                        "bytes_per_ray_step": GRID_BYTES_PER_RAY_STEP + OUT_BYTES_PER_ROW,
@@ -394,7 +405,7 @@ def gb300_arm(args, rank: int, world: int, local_rank: int):
         roofline["traffic_note"] = "scaled from a 65,536-ray x 100-step ncu capture by ray-steps"
     else:
         roofline["traffic"] = None
-        roofline["flop_note"] = "flop_per_ray_step counted by ncu on the seamount workload"
+        roofline["executed_note"] = "executed counts from ncu on the seamount workload"
     roofline["kernel_ms"] = 1e3 * kernel_s
 
     cpu = None
@@ -651,13 +662,25 @@ def batched_arm(args, rank: int, world: int, local_rank: int):
     L = mr._native.load()
     fp32_peak = ctypes.c_double()
     mr._native.check(L.mr_measure_fma_peak(0, ctypes.byref(fp32_peak)))
-    roofline = {"bound": "fp32", "achieved": None, "peak": fp32_peak.value, "unit": "TFLOP/s",
-                "frac": None, "peak_source": "measured: FP32 FMA-chain kernel on this GPU, this run",
-                "traffic": None}
-    if FP32_FLOP_PER_RAY_STEP:
-        ach = kernel_rate * FP32_FLOP_PER_RAY_STEP / 1e12
-        roofline.update({"achieved": ach, "frac": ach / fp32_peak.value,
-                         "flop_per_ray_step": FP32_FLOP_PER_RAY_STEP})
+    ach = kernel_rate * ALG_FP32_FLOP_PER_RAY_STEP / 1e12
+    roofline = {"bound": "fp32", "achieved": ach, "peak": fp32_peak.value, "unit": "TFLOP/s",
+                "frac": ach / fp32_peak.value,
+                "peak_source": "measured: FP32 FMA-chain kernel on this GPU, this run",
+                "traffic": None, "flop_per_ray_step": ALG_FP32_FLOP_PER_RAY_STEP,
+                "flop_note": "algorithmic: the reference's 270 FP64 add/mul/div and 440 f32 "
+                             "interpolation operations per ray-step, all in FP32",
+                "executed_flop_per_ray_step": FP32_FLOP_PER_RAY_STEP,
+                "executed_frac": kernel_rate * FP32_FLOP_PER_RAY_STEP / 1e12 / fp32_peak.value}
+    # DRAM bytes per ray-step of ncu captures (profiles/), scaled to one call's ray-steps
+    k2_dram_per_ray_step = {"seamount": (18.60e6 / (65536 * 400),
+                                         "65,536-ray x 400-step seamount capture"),
+                            "shelf_slope": ((394.72e6 + 37.56e6) / 331.5e6,
+                                            "4,096^2-grid, 2^20-ray x 400-step shelf-slope "
+                                            "capture")}
+    if args.workload in k2_dram_per_ray_step:
+        per, src = k2_dram_per_ray_step[args.workload]
+        roofline["traffic"] = per * done_steps / args.steps
+        roofline["traffic_note"] = f"DRAM bytes per call, scaled by ray-steps from the {src}"
     cpu = None
     if not args.no_cpu_baseline:
         if args.workload in PLAIN_WORKLOADS:
