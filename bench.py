@@ -56,9 +56,9 @@ ALG_FP32_FLOP_PER_RAY_STEP = 710.0
 # DFMA = 2), per right-hand-side arithmetic, counted by ncu on the plain
 # kernel over the seamount workload (65,536 rays x 100 steps)
 # (sm__sass_thread_inst_executed_op_d{add,mul,fma}_pred_on; profiles/).
-FP64_FLOP_PER_RAY_STEP = {"libm": 1818.1, "identity": 340.6}
+FP64_FLOP_PER_RAY_STEP = {"libm": 1818.1, "identity": 343.6}
 # FP64-pipe instructions per ray-step (sm__inst_executed_pipe_fp64 x 32, same captures)
-FP64_PIPE_INST_PER_RAY_STEP = {"libm": 1226.0, "identity": 288.7}
+FP64_PIPE_INST_PER_RAY_STEP = {"libm": 1217.9, "identity": 283.6}
 
 
 def parse():
@@ -399,9 +399,9 @@ def gb300_arm(args, rank: int, world: int, local_rank: int):
                        "bytes_per_ray_step": GRID_BYTES_PER_RAY_STEP + OUT_BYTES_PER_ROW,
                        "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"}
     # DRAM bytes of one full launch, scaled from the ncu capture of 65,536 rays
-    # x 100 steps (217.04 MB) by ray-steps (profiles/rk4_f64_seamount_65536rays_100steps.md)
+    # x 100 steps (217.03 MB) by ray-steps (profiles/rk4_f64_seamount_65536rays_100steps.md)
     if args.workload == "seamount":
-        roofline["traffic"] = 217.04e6 * ray_steps / (65536 * 100)
+        roofline["traffic"] = 217.03e6 * ray_steps / (65536 * 100)
         roofline["traffic_note"] = "scaled from a 65,536-ray x 100-step ncu capture by ray-steps"
     else:
         roofline["traffic"] = None

@@ -84,3 +84,23 @@ def test_static_entry_point_rejects_too_many_scenarios():
                       torch.cuda.current_stream())
     assert rc == N.ERR_CAPACITY
     assert b"at most 64 scenarios" in L.mr_last_error()
+
+
+def test_static_entry_point_rejects_ray_ordering():
+    # ordering needs scratch memory: the static entry point refuses it
+    import torch
+
+    import mantaray_gb300 as mr
+    from mantaray_gb300 import _native as N
+    from mantaray_gb300.batch import BatchTracer, make_config
+
+    L = N.load()
+    x = np.arange(4, dtype=np.float32) * 10.0
+    tracer = BatchTracer([(mr.Bathymetry.grid(x, x, np.full(16, 100.0)),
+                           mr.Current.constant(0.0, 0.0))])
+    ins = [torch.full((8,), v, dtype=torch.float64, device="cuda") for v in (5.0, 5.0, 0.05, 0.0)]
+    out = BatchTracer.alloc(8, 10, 0)
+    rc = _static_call(L, N, tracer, ins, 1.0, 10, 0, out, make_config(128, 4, 1, 32, 1),
+                      torch.cuda.current_stream())
+    assert rc == N.ERR_INVALID_ARGUMENT
+    assert b"ordering" in L.mr_last_error()
