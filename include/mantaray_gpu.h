@@ -299,7 +299,8 @@ int mr_diff_forward(int precision, const mr_diff_grid *bgrid, const void *depth,
 /* Given grad_end [4][n] = dL/d(end state), writes grad_state0 [4][n] =
  * dL/d(initial state) and sets grad_depth [bny*bnx], grad_u, grad_v
  * [cny*cnx] (f64) to dL/d(node).  Rays with status != 0 contribute nothing.
- * segment: scratch [checkpoint_every][4][n]. */
+ * segment: scratch [checkpoint_every][16][n] (every step's four RK4 stage
+ * states). */
 int mr_diff_backward(int precision, const mr_diff_grid *bgrid, const void *depth,
                      const mr_diff_grid *cgrid, const void *u, const void *v,
                      size_t n, const void *x0, const void *y0, const void *kx0,

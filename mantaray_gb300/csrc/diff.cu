@@ -24,8 +24,9 @@
 // adjoint step backward (VJP), both through the four RK4 stages.
 //
 // Adjoint pass per ray: the forward stored the state every C steps; each
-// segment is recomputed from its checkpoint into a scratch buffer and walked
-// backward.  Gradients with respect to grid nodes are accumulated per ray
+// segment is recomputed from its checkpoint into a scratch buffer (every
+// step's four stage states) and walked backward, evaluating each stage's
+// partials where its transpose is applied.  Gradients with respect to grid nodes are accumulated per ray
 // while the ray stays in one cell, then added to the node arrays with FP64
 // atomics, aggregated across the lanes of a warp that flush the same cell.
 // The per-cell accumulation runs in the working precision; only the
@@ -61,7 +62,7 @@ struct DiffArgs {
   uint8_t *status;      // [n]
   // adjoint
   const T *grad_end;    // [4][n]
-  T *seg;               // [ck_every][4][n]
+  T *seg;               // [ck_every][16][n]: y and the stage states Y2, Y3, Y4
   T *grad_state0;       // [4][n]
   double *grad_depth;   // [bny*bnx]
   double *grad_u, *grad_v;  // [cny*cnx]
@@ -416,13 +417,10 @@ __global__ void __launch_bounds__(64) diff_tangent_kernel(DiffArgs<T> A) {
   A.status[i] = ok ? 0 : 1;
 }
 
-// FP64 keeps the four stages' partials per backward step; FP32 re-evaluates
-// them (its right-hand side is cheap and the registers bound its occupancy).
+// FP32: capped at 96 registers (10 blocks of 64 per SM; measured fastest of
+// 8 / 10 / 12); FP64 uses what it needs (242).
 template <typename T>
-constexpr bool kStorePoints = sizeof(T) == 8;
-
-template <typename T>
-__global__ void __launch_bounds__(64) diff_adjoint_kernel(DiffArgs<T> A) {
+__global__ void __launch_bounds__(64, sizeof(T) == 4 ? 10 : 1) diff_adjoint_kernel(DiffArgs<T> A) {
   const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= A.n) return;
   if (A.status[i] != 0) {  // no gradient through a ray that stopped
@@ -437,81 +435,72 @@ __global__ void __launch_bounds__(64) diff_adjoint_kernel(DiffArgs<T> A) {
   acc.bkey = acc.ckey = -1;
 #pragma unroll
   for (int q = 0; q < 4; ++q) acc.d[q] = acc.u[q] = acc.v[q] = T(0);
-  const T half = A.dt * T(0.5), h = A.dt;
+  const T half = A.dt * T(0.5), h = A.dt, sixth = A.dt / T(6);
   for (int64_t seg = A.n_ck - 1; seg >= 0; --seg) {
     const int64_t first = seg * A.ck_every;
     const int64_t last = min(first + A.ck_every, A.steps);  // steps [first, last)
-    // recompute the segment's states from its checkpoint
+    // recompute the segment from its checkpoint, keeping every step's four
+    // stage states (y, Y2, Y3, Y4) in the scratch
     T y[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) y[q] = A.ckpt[(seg * 4 + q) * A.n + i];
     for (int64_t s = first; s < last; ++s) {
-#pragma unroll
-      for (int q = 0; q < 4; ++q) A.seg[((s - first) * 4 + q) * A.n + i] = y[q];
-      if (s + 1 < last) rk4(A, y);
-    }
-    // walk it backward
-    for (int64_t s = last - 1; s >= first; --s) {
-#pragma unroll
-      for (int q = 0; q < 4; ++q) y[q] = A.seg[((s - first) * 4 + q) * A.n + i];
+      Point<T> P;
       T k1[4], k2[4], k3[4], k4[4], Y2[4], Y3[4], Y4[4];
-      T w[4], r4[4], r3[4], r2[4], r1[4];
-      if (kStorePoints<T>) {
-        // keep the four stages' partials (registers are traded for
-        // right-hand-side evaluations where those are expensive: FP64)
-        Point<T> P1, P2, P3, P4;
-        eval(A, y, P1, k1);
+      eval(A, y, P, k1);
 #pragma unroll
-        for (int q = 0; q < 4; ++q) Y2[q] = y[q] + k1[q] * half;
-        eval(A, Y2, P2, k2);
+      for (int q = 0; q < 4; ++q) Y2[q] = y[q] + k1[q] * half;
+      eval(A, Y2, P, k2);
 #pragma unroll
-        for (int q = 0; q < 4; ++q) Y3[q] = y[q] + k2[q] * half;
-        eval(A, Y3, P3, k3);
+      for (int q = 0; q < 4; ++q) Y3[q] = y[q] + k2[q] * half;
+      eval(A, Y3, P, k3);
 #pragma unroll
-        for (int q = 0; q < 4; ++q) Y4[q] = y[q] + k3[q] * h;
-        eval(A, Y4, P4, k4);
+      for (int q = 0; q < 4; ++q) Y4[q] = y[q] + k3[q] * h;
+      T *row = A.seg + (s - first) * 16 * A.n + i;
 #pragma unroll
-        for (int q = 0; q < 4; ++q) w[q] = lam[q] * (h / T(6));
-        vjp(A, Y4, P4, w, r4, acc);
-#pragma unroll
-        for (int q = 0; q < 4; ++q) w[q] = lam[q] * (h / T(3)) + h * r4[q];
-        vjp(A, Y3, P3, w, r3, acc);
-#pragma unroll
-        for (int q = 0; q < 4; ++q) w[q] = lam[q] * (h / T(3)) + half * r3[q];
-        vjp(A, Y2, P2, w, r2, acc);
-#pragma unroll
-        for (int q = 0; q < 4; ++q) w[q] = lam[q] * (h / T(6)) + half * r2[q];
-        vjp(A, y, P1, w, r1, acc);
-      } else {
-        // keep only the stage states and evaluate each stage again when its
-        // transpose is applied: one live Point, far fewer registers
-        Point<T> P;
-        eval(A, y, P, k1);
-#pragma unroll
-        for (int q = 0; q < 4; ++q) Y2[q] = y[q] + k1[q] * half;
-        eval(A, Y2, P, k2);
-#pragma unroll
-        for (int q = 0; q < 4; ++q) Y3[q] = y[q] + k2[q] * half;
-        eval(A, Y3, P, k3);
-#pragma unroll
-        for (int q = 0; q < 4; ++q) Y4[q] = y[q] + k3[q] * h;
+      for (int q = 0; q < 4; ++q) {
+        row[q * A.n] = y[q];
+        row[(4 + q) * A.n] = Y2[q];
+        row[(8 + q) * A.n] = Y3[q];
+        row[(12 + q) * A.n] = Y4[q];
+      }
+      if (s + 1 < last) {
         eval(A, Y4, P, k4);
 #pragma unroll
-        for (int q = 0; q < 4; ++q) w[q] = lam[q] * (h / T(6));
-        vjp(A, Y4, P, w, r4, acc);
-        eval(A, Y3, P, k3);
-#pragma unroll
-        for (int q = 0; q < 4; ++q) w[q] = lam[q] * (h / T(3)) + h * r4[q];
-        vjp(A, Y3, P, w, r3, acc);
-        eval(A, Y2, P, k2);
-#pragma unroll
-        for (int q = 0; q < 4; ++q) w[q] = lam[q] * (h / T(3)) + half * r3[q];
-        vjp(A, Y2, P, w, r2, acc);
-        eval(A, y, P, k1);
-#pragma unroll
-        for (int q = 0; q < 4; ++q) w[q] = lam[q] * (h / T(6)) + half * r2[q];
-        vjp(A, y, P, w, r1, acc);
+        for (int q = 0; q < 4; ++q)
+          y[q] = y[q] + (((k1[q] + k2[q] * T(2)) + k3[q] * T(2)) + k4[q]) * sixth;
       }
+    }
+    // walk it backward: each stage's partials are evaluated where its
+    // transpose is applied (one live Point)
+    for (int64_t s = last - 1; s >= first; --s) {
+      const T *row = A.seg + (s - first) * 16 * A.n + i;
+      Point<T> P;
+      T Ys[4], kd[4], w[4], r4[4], r3[4], r2[4], r1[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) Ys[q] = row[(12 + q) * A.n];
+      eval(A, Ys, P, kd);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) w[q] = lam[q] * (h / T(6));
+      vjp(A, Ys, P, w, r4, acc);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) Ys[q] = row[(8 + q) * A.n];
+      eval(A, Ys, P, kd);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) w[q] = lam[q] * (h / T(3)) + h * r4[q];
+      vjp(A, Ys, P, w, r3, acc);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) Ys[q] = row[(4 + q) * A.n];
+      eval(A, Ys, P, kd);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) w[q] = lam[q] * (h / T(3)) + half * r3[q];
+      vjp(A, Ys, P, w, r2, acc);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) Ys[q] = row[q * A.n];
+      eval(A, Ys, P, kd);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) w[q] = lam[q] * (h / T(6)) + half * r2[q];
+      vjp(A, Ys, P, w, r1, acc);
 #pragma unroll
       for (int q = 0; q < 4; ++q) lam[q] = lam[q] + r1[q] + r2[q] + r3[q] + r4[q];
     }

@@ -94,7 +94,7 @@ class _Endpoints:
                 n = x0.numel()
                 p = _precision(x0)
                 grad_end = grad_end.contiguous().to(x0.dtype)
-                seg = torch.empty((every, 4, n), dtype=x0.dtype, device=x0.device)
+                seg = torch.empty((every, 16, n), dtype=x0.dtype, device=x0.device)
                 g0 = torch.empty((4, n), dtype=x0.dtype, device=x0.device)
                 gd = torch.empty((bgrid.ny, bgrid.nx), dtype=torch.float64, device=x0.device)
                 gu = torch.empty((cgrid.ny, cgrid.nx), dtype=torch.float64, device=x0.device)
