@@ -137,6 +137,16 @@ __device__ __forceinline__ float bilin(const float4 &v, float fx, float fy) {
   return fmaf(fy, b - a, a);
 }
 
+// The cell records a lane read last, kept in registers: a ray stays in one
+// cell for several steps, so most stage lookups reuse them instead of
+// loading them again (same values, no memory latency on the dependent chain).
+struct CellCache {
+  int64_t bkey, ckey;     // cell indices held, -1: none
+  float4 b0;              // depth corners
+  float bx, by;           // dh/dx, dh/dy
+  float4 c0, c1, c2;      // u corners, v corners, gradients
+};
+
 struct RayLane {
   int64_t ray;      // -1: empty slot, -2: no work left
   int scen;
@@ -148,28 +158,38 @@ struct RayLane {
   int32_t saved;
   int32_t to_save;    // steps until the next decimated row (no 64-bit modulo per step)
   int32_t to_rebase;  // steps until the next origin rebase
+  CellCache cache;
 };
 
 // Right-hand side in FP32 at offset (px, py); returns a BatchStatus.
-__device__ __forceinline__ int rhs_f32(const ScenarioDev &s, const RayLane &L, float px, float py,
+__device__ __forceinline__ int rhs_f32(const ScenarioDev &s, RayLane &L, float px, float py,
                                        float kx, float ky, float d[4]) {
   int64_t cb;
   float fx, fy;
   if (!locate(s.bathy, L.pb, px, py, &cb, &fx, &fy)) return BATCH_OUT_OF_DOMAIN;
-  const float4 b0 = __ldg(s.bathy.cells + 2 * cb);
-  const float4 b1 = __ldg(s.bathy.cells + 2 * cb + 1);
-  const float h = bilin(b0, fx, fy);
+  CellCache &C = L.cache;
+  if (cb != C.bkey) {
+    C.b0 = __ldg(s.bathy.cells + 2 * cb);
+    const float4 b1 = __ldg(s.bathy.cells + 2 * cb + 1);
+    C.bx = b1.x;
+    C.by = b1.y;
+    C.bkey = cb;
+  }
+  const float h = bilin(C.b0, fx, fy);
   float u, v, dudx = 0.0f, dudy = 0.0f, dvdx = 0.0f, dvdy = 0.0f;
   if (s.current.kind == 0) {
     int64_t cc;
     float gx, gy;
     if (!locate(s.current, L.pc, px, py, &cc, &gx, &gy)) return BATCH_OUT_OF_DOMAIN;
-    const float4 c0 = __ldg(s.current.cells + 3 * cc);
-    const float4 c1 = __ldg(s.current.cells + 3 * cc + 1);
-    const float4 c2 = __ldg(s.current.cells + 3 * cc + 2);
-    u = bilin(c0, gx, gy);
-    v = bilin(c1, gx, gy);
-    dudx = c2.x; dudy = c2.y; dvdx = c2.z; dvdy = c2.w;
+    if (cc != C.ckey) {
+      C.c0 = __ldg(s.current.cells + 3 * cc);
+      C.c1 = __ldg(s.current.cells + 3 * cc + 1);
+      C.c2 = __ldg(s.current.cells + 3 * cc + 2);
+      C.ckey = cc;
+    }
+    u = bilin(C.c0, gx, gy);
+    v = bilin(C.c1, gx, gy);
+    dudx = C.c2.x; dudy = C.c2.y; dvdx = C.c2.z; dvdy = C.c2.w;
   } else {
     u = s.current.cu;
     v = s.current.cv;
@@ -193,8 +213,8 @@ __device__ __forceinline__ int rhs_f32(const ScenarioDev &s, const RayLane &L, f
   const float f = -0.5f * k * inv_shch * (gkt * rs);
   d[0] = fmaf(cg, kx * rk, u);
   d[1] = fmaf(cg, ky * rk, v);
-  d[2] = fmaf(-ky, dvdx, fmaf(-kx, dudx, f * b1.x));
-  d[3] = fmaf(-ky, dvdy, fmaf(-kx, dudy, f * b1.y));
+  d[2] = fmaf(-ky, dvdx, fmaf(-kx, dudx, f * C.bx));
+  d[3] = fmaf(-ky, dvdy, fmaf(-kx, dudy, f * C.by));
   return BATCH_COMPLETE;
 }
 
@@ -257,6 +277,7 @@ __device__ __forceinline__ void start(const BatchArgs &a, RayLane &L, int64_t r)
   L.pc = grid_pos(s.current, L.ox, L.oy);
   L.step = 0;
   L.saved = 0;
+  L.cache.bkey = L.cache.ckey = -1;
   L.to_save = save_period(a);
   L.to_rebase = a.rebase_interval;
   if (a.decimation > 0) {
