@@ -104,7 +104,9 @@ def cpu_threads() -> int:
 def cpu_sample(w, seconds: float, threads: int):
     """Times the oracle (CPU restatement of the reference path, OpenMP over
     rays) on successive batches of the workload's rays until `seconds` pass.
-    Returns (ray-steps/s, description)."""
+    After a first batch of 16 rays per thread the batches grow to fill the
+    remaining time, so one long ray does not leave the other threads idle at
+    the end of every batch.  Returns (ray-steps/s, description, seconds)."""
     from oracle import pyoracle
 
     ob = pyoracle.Bathymetry.grid(w.bx, w.by, w.depth)
@@ -112,20 +114,28 @@ def cpu_sample(w, seconds: float, threads: int):
     batch = max(threads * 16, 256)
     done_rays = 0
     ray_steps = 0
+    sizes = []
     t_start = time.perf_counter()
     i = 0
     while True:
         idx = np.arange(i, i + batch) % w.n
+        t_b = time.perf_counter()
         traj, n_rows, _ = pyoracle.trace(ob, oc, w.x0[idx], w.y0[idx], w.kx0[idx], w.ky0[idx],
                                          w.t0, w.t_end, w.dt, threads=threads)
+        t_b = time.perf_counter() - t_b
         ray_steps += int(np.sum(n_rows.astype(np.int64) - 1))
         done_rays += batch
+        sizes.append(batch)
         i += batch
         elapsed = time.perf_counter() - t_start
         if elapsed >= seconds:
             break
-    desc = (f"{done_rays} of the workload's rays (batches of {batch}) x up to "
-            f"{int(round((w.t_end - w.t0) / w.dt))} steps with full trajectories, "
+        # next batch: about half the remaining time, within memory bounds
+        rows = int(round((w.t_end - w.t0) / w.dt)) + 1
+        cap = max(256, int(2e9 // (5 * 8 * rows)))
+        batch = int(min(cap, max(batch, batch * 0.5 * (seconds - elapsed) / max(t_b, 1e-3))))
+    desc = (f"{done_rays} of the workload's rays (batches of {min(sizes)} to {max(sizes)}) x up "
+            f"to {int(round((w.t_end - w.t0) / w.dt))} steps with full trajectories, "
             f"{threads} OpenMP threads, {elapsed:.1f} s wall")
     return ray_steps / elapsed, desc, elapsed
 

@@ -33,6 +33,7 @@ struct PackedGrid {
 struct ScenarioDev {
   PackedGrid bathy;      // 2 float4 per cell
   PackedGrid current;    // 3 float4 per cell
+  int same_grid;         // gridded current on the bathymetry's grid: one cell lookup serves both
 };
 
 // Per-ray termination status of the batched form.

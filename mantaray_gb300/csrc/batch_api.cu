@@ -256,6 +256,14 @@ int mr_batch_create(size_t n_scenarios, const mr_bathymetry *const *bathy,
   for (size_t i = 0; i < n_scenarios && rc == MR_OK; ++i) {
     rc = pack_bathy(b, bathy[i], &b->host_scen[i].bathy, s);
     if (rc == MR_OK) rc = pack_current(b, current[i], &b->host_scen[i].current, s);
+    if (rc == MR_OK) {
+      const mr::PackedGrid &gb = b->host_scen[i].bathy, &gc = b->host_scen[i].current;
+      b->host_scen[i].same_grid =
+          gc.kind == 0 && gb.nx == gc.nx && gb.ny == gc.ny && gb.x0 == gc.x0 &&
+          gb.y0 == gc.y0 && gb.sp_x == gc.sp_x && gb.sp_y == gc.sp_y &&
+          gb.inv_sp_x == gc.inv_sp_x && gb.inv_sp_y == gc.inv_sp_y &&
+          gb.inv_sp_xd == gc.inv_sp_xd && gb.inv_sp_yd == gc.inv_sp_yd;
+    }
   }
   cudaError_t e = cudaSuccess;
   if (rc == MR_OK) e = cudaMalloc(reinterpret_cast<void **>(&b->scen), n_scenarios * sizeof(mr::ScenarioDev));

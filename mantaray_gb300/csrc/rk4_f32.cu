@@ -178,9 +178,10 @@ __device__ __forceinline__ int rhs_f32(const ScenarioDev &s, RayLane &L, float p
   const float h = bilin(C.b0, fx, fy);
   float u, v, dudx = 0.0f, dudy = 0.0f, dvdx = 0.0f, dvdy = 0.0f;
   if (s.current.kind == 0) {
-    int64_t cc;
-    float gx, gy;
-    if (!locate(s.current, L.pc, px, py, &cc, &gx, &gy)) return BATCH_OUT_OF_DOMAIN;
+    int64_t cc = cb;
+    float gx = fx, gy = fy;  // the same cell when the grids coincide (same origin, same arithmetic)
+    if (!s.same_grid && !locate(s.current, L.pc, px, py, &cc, &gx, &gy))
+      return BATCH_OUT_OF_DOMAIN;
     if (cc != C.ckey) {
       C.c0 = __ldg(s.current.cells + 3 * cc);
       C.c1 = __ldg(s.current.cells + 3 * cc + 1);
@@ -202,7 +203,7 @@ __device__ __forceinline__ int rhs_f32(const ScenarioDev &s, RayLane &L, float p
   const float kh = k * h;
   const float m = -expm1f(-2.0f * kh);  // 1 - exp(-2kh)
   const float q = 1.0f - m;
-  const float inv_d = 1.0f / (m * (2.0f - m));
+  const float inv_d = __frcp_rn(m * (2.0f - m));  // = 1.0f / x, correctly rounded
   const float r = m * inv_d;            // 1 / (2 - m)
   const float th = m * r;               // tanh(kh)
   const float kh_ch2 = 4.0f * kh * q * r * r;
@@ -230,7 +231,7 @@ __device__ __forceinline__ void rebase(const ScenarioDev &s, RayLane &L) {
   L.oy += static_cast<double>(L.py) - static_cast<double>(L.cpy);
   L.px = L.py = L.cpx = L.cpy = 0.0f;
   L.pb = grid_pos(s.bathy, L.ox, L.oy);
-  L.pc = grid_pos(s.current, L.ox, L.oy);
+  L.pc = s.same_grid ? L.pb : grid_pos(s.current, L.ox, L.oy);
 }
 
 __device__ __forceinline__ void save_row(const BatchArgs &a, const RayLane &L) {
@@ -274,7 +275,7 @@ __device__ __forceinline__ void start(const BatchArgs &a, RayLane &L, int64_t r)
   L.kx = static_cast<float>(a.kx0[r]);
   L.ky = static_cast<float>(a.ky0[r]);
   L.pb = grid_pos(s.bathy, L.ox, L.oy);
-  L.pc = grid_pos(s.current, L.ox, L.oy);
+  L.pc = s.same_grid ? L.pb : grid_pos(s.current, L.ox, L.oy);
   L.step = 0;
   L.saved = 0;
   L.cache.bkey = L.cache.ckey = -1;
