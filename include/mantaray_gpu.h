@@ -224,7 +224,9 @@ void mr_batch_destroy(mr_batch *b);
  * ray_scenario [n] (null: all scenario 0); x0, y0, kx0, ky0 [n];
  * saved [5][save_cap][n] f32 (t, x, y, kx, ky) every `decimation` steps, step
  * 0 included (decimation 0: no rows; rows a ray does not reach are NaN);
- * end_state [5][n] f64; n_steps, n_saved [n]; status [n]. */
+ * end_state [5][n] f64; n_steps, n_saved [n]; status [n].  Inputs are device
+ * memory; outputs device memory or page-locked host memory, which the kernel
+ * writes in place (the decimated rows then reach the host while it runs). */
 int mr_batch_trace_device(mr_batch *b, size_t n, const uint8_t *ray_scenario,
                           const double *x0, const double *y0, const double *kx0,
                           const double *ky0, double t0, double dt,

@@ -39,7 +39,8 @@ def make_config(block=128, blocks_per_sm=4, rays_per_lane=1, rebase_interval=32,
 
 @dataclass
 class BatchResult:
-    """Outputs of one batched call (torch CUDA tensors)."""
+    """Outputs of one batched call: torch CUDA tensors, or page-locked CPU
+    tensors (`pin_memory()`), which the kernel writes in place."""
 
     saved: object       # [5][save_cap][n] f32 (t, x, y, kx, ky), NaN past each ray's rows
     end_state: object   # [5][n] f64 last valid state

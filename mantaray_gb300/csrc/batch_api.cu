@@ -158,6 +158,23 @@ int check_config(const mr_batch_config *cfg) {
   return MR_OK;
 }
 
+// The device address of an output buffer: device memory as given,
+// page-locked host memory through its device mapping; null for pageable host
+// memory (not writable from the kernel).
+template <typename T>
+T *device_view(T *p) {
+  if (!p) return p;
+  cudaPointerAttributes attr;
+  if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged) return p;
+  if (attr.type == cudaMemoryTypeHost && attr.devicePointer)
+    return static_cast<T *>(attr.devicePointer);
+  return nullptr;
+}
+
 int fill_args(mr_batch *b, size_t n, size_t n_stride, const uint8_t *ray_scenario,
               const double *x0, const double *y0, const double *kx0, const double *ky0, double t0,
               double dt, int64_t max_steps, int64_t decimation, size_t save_cap, float *saved,
@@ -190,11 +207,16 @@ int fill_args(mr_batch *b, size_t n, size_t n_stride, const uint8_t *ray_scenari
   a->save_cap = static_cast<int64_t>(save_cap);
   a->n_stride = static_cast<int64_t>(n_stride);
   a->rebase_interval = cfg->rebase_interval;
-  a->saved = saved;
-  a->end_state = end_state;
-  a->n_steps = n_steps;
-  a->n_saved = n_saved;
-  a->status = status;
+  // outputs: device memory or page-locked host memory (written in place)
+  a->saved = decimation > 0 ? device_view(saved) : saved;
+  a->end_state = device_view(end_state);
+  a->n_steps = device_view(n_steps);
+  a->n_saved = device_view(n_saved);
+  a->status = device_view(status);
+  if (n_stride > 0 && (!a->end_state || !a->n_steps || !a->n_saved || !a->status ||
+                       (decimation > 0 && !a->saved)))
+    return fail(MR_ERR_INVALID_ARGUMENT,
+                "outputs must be device memory or page-locked host memory");
   a->queue = b->queue;
   return MR_OK;
 }
@@ -207,7 +229,7 @@ cudaError_t enqueue(const mr_batch *b, mr::BatchArgs a, const mr_batch_config *c
   cudaError_t e = cudaMemsetAsync(a.queue, 0, sizeof(unsigned long long), s);
   if (e != cudaSuccess) return e;
   if (a.decimation > 0 && a.save_cap > 0) {
-    e = cudaMemsetAsync(a.saved, 0xFF, sizeof(float) * 5 * a.save_cap * a.n_stride, s);
+    e = mr::launch_fill_nan(a.saved, 5 * a.save_cap * a.n_stride, s);
     if (e != cudaSuccess) return e;
   }
   a.order = nullptr;

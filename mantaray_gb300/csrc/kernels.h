@@ -34,6 +34,7 @@ cudaError_t launch_pack_current(const CurrentDev &c, float4 *cells, cudaStream_t
 cudaError_t launch_rk4_f32(const BatchArgs &a, int block, int blocks_per_sm, int rays_per_lane,
                            cudaStream_t stream);
 const void *rk4_f32_function(int rays_per_lane);
+cudaError_t launch_fill_nan(float *p, int64_t count, cudaStream_t stream);
 
 // Spatial ordering of a batched call's rays (K6): sorts by key in `passes`
 // 8-bit digits; the order is then o.vals[passes & 1].  Grids are sized for

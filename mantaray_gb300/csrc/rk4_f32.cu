@@ -382,6 +382,29 @@ cudaError_t launch_pack_current(const CurrentDev &c, float4 *cells, cudaStream_t
   return cudaGetLastError();
 }
 
+// NaN fill of the decimated rows (a kernel, so that it writes page-locked
+// host buffers through their device mapping as well as device memory).
+namespace {
+__global__ void fill_nan_kernel(float *p, int64_t count) {
+  const float nan = __int_as_float(0x7fffffff);
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < count;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    p[i] = nan;
+}
+}  // namespace
+
+cudaError_t launch_fill_nan(float *p, int64_t count, cudaStream_t stream) {
+  if (count <= 0) return cudaSuccess;
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  const int64_t blocks = (count + 255) / 256;
+  const unsigned grid = static_cast<unsigned>(blocks < 8ll * sms ? blocks : 8ll * sms);
+  fill_nan_kernel<<<grid, 256, 0, stream>>>(p, count);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_rk4_f32(const BatchArgs &a, int block, int blocks_per_sm, int rays_per_lane,
                            cudaStream_t stream) {
   int dev = 0, sms = 0;

@@ -227,3 +227,46 @@ def test_rays_outnumber_lanes_and_queue_drains(mr):
     last_finite = np.where(status.cpu().numpy() == 0, rows - 1, rows - 2)
     assert np.mean(np.abs(steps - last_finite) <= 1) >= 0.999
     assert len(np.unique(steps)) > 10  # uneven lifetimes
+
+
+def test_page_locked_host_outputs_are_written_in_place(mr):
+    # outputs in page-locked host memory: the kernel writes them through
+    # their device mapping; results equal the device-buffer call's
+    import torch
+
+    from mantaray_gb300.batch import BatchResult, BatchTracer
+    from mantaray_gb300.workloads import seamount
+
+    w = seamount(n_rays=2048, steps=300)
+    b, c = _fields(mr, w)
+    tracer = BatchTracer([(b, c)])
+    x0, y0, kx0, ky0 = _dev(w.x0, w.y0, w.kx0, w.ky0)
+    ref = tracer.trace(x0, y0, kx0, ky0, w.dt, 300, decimation=25)
+    dev_out = BatchTracer.alloc(2048, 300, 25)
+    host = BatchResult(*(torch.full_like(t, 3, device="cpu").pin_memory() for t in
+                         (dev_out.saved, dev_out.end_state, dev_out.n_steps, dev_out.n_saved,
+                          dev_out.status)))
+    tracer.trace(x0, y0, kx0, ky0, w.dt, 300, decimation=25, out=host)
+    torch.cuda.synchronize()
+    for a, b_ in zip((ref.saved, ref.end_state, ref.n_steps, ref.n_saved, ref.status),
+                     (host.saved, host.end_state, host.n_steps, host.n_saved, host.status)):
+        np.testing.assert_array_equal(np.nan_to_num(a.cpu().numpy(), nan=-7.0),
+                                      np.nan_to_num(b_.numpy(), nan=-7.0))
+
+
+def test_pageable_host_outputs_are_refused(mr):
+    import torch
+
+    from mantaray_gb300 import MantarayError
+    from mantaray_gb300.batch import BatchResult, BatchTracer
+    from mantaray_gb300.workloads import seamount
+
+    w = seamount(n_rays=64, steps=10)
+    b, c = _fields(mr, w)
+    tracer = BatchTracer([(b, c)])
+    x0, y0, kx0, ky0 = _dev(w.x0, w.y0, w.kx0, w.ky0)
+    d = BatchTracer.alloc(64, 10, 0)
+    bad = BatchResult(d.saved, torch.zeros_like(d.end_state, device="cpu"), d.n_steps,
+                      d.n_saved, d.status)
+    with pytest.raises(MantarayError, match="page-locked"):
+        tracer.trace(x0, y0, kx0, ky0, w.dt, 10, out=bad)
