@@ -61,6 +61,8 @@ __global__ void __launch_bounds__(kK1Block) rk4_f64_kernel(BathyDev b, CurrentDe
   constexpr bool F = Rhs::kFma;
   const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   const bool valid = i < a.n;
+  // lanes present in this warp (blocks may be smaller than a warp)
+  const unsigned warp_mask = blockDim.x >= 32 ? 0xffffffffu : (1u << blockDim.x) - 1u;
   const uint64_t plane = a.rows_cap * a.n;
   double y[4] = {0.0, 0.0, 0.0, 0.0};
   double k1[4] = {0.0, 0.0, 0.0, 0.0};
@@ -78,7 +80,7 @@ __global__ void __launch_bounds__(kK1Block) rk4_f64_kernel(BathyDev b, CurrentDe
   uint64_t s = 0;
   for (; s < a.nsteps; ++s) {
     // Once every lane of the warp has stopped, the rest is NaN padding.
-    if (__all_sync(0xffffffffu, !alive)) break;
+    if (__all_sync(warp_mask, !alive)) break;
     if (alive) {
       double acc[4], kc[4], yn[4];
 #pragma unroll
@@ -128,17 +130,26 @@ __global__ void __launch_bounds__(kK1Block) rk4_f64_kernel(BathyDev b, CurrentDe
 cudaError_t launch_rk4_f64(const BathyDev &b, const CurrentDev &c, const TraceArgs &a,
                            int stop_rule, int identity_math, cudaStream_t stream) {
   if (a.n == 0) return cudaSuccess;
-  const unsigned grid = static_cast<unsigned>((a.n + kK1Block - 1) / kK1Block);
+  // Blocks of 64 rays, or fewer when that leaves SMs without a block: on
+  // GB300 an SM issues 2 FP64 lanes per clock, so a small call runs fastest
+  // with its rays spread over as many SMs as possible (down to 8 per block).
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  int block = kK1Block;
+  while (block > 8 && (a.n + block - 1) / block < static_cast<uint64_t>(sms)) block /= 2;
+  const unsigned grid = static_cast<unsigned>((a.n + block - 1) / block);
   if (identity_math) {
     if (stop_rule == 1)
-      rk4_f64_kernel<1, RhsIdentity><<<grid, kK1Block, 0, stream>>>(b, c, a);
+      rk4_f64_kernel<1, RhsIdentity><<<grid, block, 0, stream>>>(b, c, a);
     else
-      rk4_f64_kernel<0, RhsIdentity><<<grid, kK1Block, 0, stream>>>(b, c, a);
+      rk4_f64_kernel<0, RhsIdentity><<<grid, block, 0, stream>>>(b, c, a);
   } else {
     if (stop_rule == 1)
-      rk4_f64_kernel<1, RhsLibm><<<grid, kK1Block, 0, stream>>>(b, c, a);
+      rk4_f64_kernel<1, RhsLibm><<<grid, block, 0, stream>>>(b, c, a);
     else
-      rk4_f64_kernel<0, RhsLibm><<<grid, kK1Block, 0, stream>>>(b, c, a);
+      rk4_f64_kernel<0, RhsLibm><<<grid, block, 0, stream>>>(b, c, a);
   }
   return cudaGetLastError();
 }
