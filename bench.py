@@ -43,7 +43,7 @@ GRID_BYTES_PER_RAY_STEP = 4 * 3 * 4 * 8
 OUT_BYTES_PER_ROW = 5 * 8
 # FP32 floating-point operations one ray-step of the batched kernel executes
 # (FADD/FMUL = 1, FFMA = 2), counted by ncu on the seamount workload.
-FP32_FLOP_PER_RAY_STEP = 539.2
+FP32_FLOP_PER_RAY_STEP = 487.4
 # Algorithmic work of one ray-step (the reference's arithmetic, hand count from
 # src/wave_ray_path.rs:118-216 plus the RK4 update): ~55 FP64 add/mul/div per
 # right-hand side x 4 + ~53 for the update = 270 (36 transcendental calls not
@@ -684,13 +684,14 @@ def batched_arm(args, rank: int, world: int, local_rank: int):
                 "peak_source": "measured: FP32 FMA-chain kernel on this GPU, this run",
                 "traffic": None, "flop_per_ray_step": ALG_FP32_FLOP_PER_RAY_STEP,
                 "flop_note": "algorithmic: the reference's 270 FP64 add/mul/div and 440 f32 "
-                             "interpolation operations per ray-step, all in FP32",
+                             "interpolation operations per ray-step, all in FP32; executed: ncu "
+                             "count with the current on the bathymetry's grid",
                 "executed_flop_per_ray_step": FP32_FLOP_PER_RAY_STEP,
                 "executed_frac": kernel_rate * FP32_FLOP_PER_RAY_STEP / 1e12 / fp32_peak.value}
     # DRAM bytes per ray-step of ncu captures (profiles/), scaled to one call's ray-steps
     k2_dram_per_ray_step = {"seamount": (18.60e6 / (65536 * 400),
                                          "65,536-ray x 400-step seamount capture"),
-                            "shelf_slope": ((386.89e6 + 37.00e6) / 331.5e6,
+                            "shelf_slope": ((371.45e6 + 36.64e6) / 331.5e6,
                                             "4,096^2-grid, 2^20-ray x 400-step shelf-slope "
                                             "capture")}
     if args.workload in k2_dram_per_ray_step:
