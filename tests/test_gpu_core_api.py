@@ -65,6 +65,21 @@ def test_multiple_rays(mr, files):
     assert (ds.ky == 0.0).all()
 
 
+def test_identity_math_through_the_drop_in(mr, oracle, files):
+    # the faster arithmetic through the reference-shaped call: same rows,
+    # values within the parity bar of the default (libm) call
+    x0, y0 = [-1000.0, 200.0, 3000.0], [0.0, -500.0, 250.0]
+    kx0, ky0 = [0.01, 0.02, 0.005], [0.0, 0.01, -0.01]
+    a = mr.ray_tracing(x0, y0, kx0, ky0, 200, 1, str(files[0]), str(files[1]))
+    b = mr.ray_tracing(x0, y0, kx0, ky0, 200, 1, str(files[0]), str(files[1]), math="identity")
+    assert a.sizes == b.sizes
+    for v in ("x", "y", "kx", "ky"):
+        va, vb = np.asarray(a[v]), np.asarray(b[v])
+        np.testing.assert_array_equal(np.isnan(va), np.isnan(vb))
+        ok = np.isfinite(va)
+        assert np.all(np.abs(va[ok] - vb[ok]) <= 1e-9 * np.maximum(np.abs(va[ok]), 1e-6))
+
+
 def test_rays_variable_length(mr, oracle, files):
     # python/tests/test_core.py:81-101 (no assertion there): one ray reaches
     # the grid edge first; the shorter ray is NaN padded to the longer one.
