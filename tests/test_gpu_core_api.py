@@ -73,11 +73,11 @@ def test_identity_math_through_the_drop_in(mr, oracle, files):
     a = mr.ray_tracing(x0, y0, kx0, ky0, 200, 1, str(files[0]), str(files[1]))
     b = mr.ray_tracing(x0, y0, kx0, ky0, 200, 1, str(files[0]), str(files[1]), math="identity")
     assert a.sizes == b.sizes
-    for v in ("x", "y", "kx", "ky"):
+    for v, floor in (("x", 1.0), ("y", 1.0), ("kx", 1e-6), ("ky", 1e-6)):
         va, vb = np.asarray(a[v]), np.asarray(b[v])
         np.testing.assert_array_equal(np.isnan(va), np.isnan(vb))
         ok = np.isfinite(va)
-        assert np.all(np.abs(va[ok] - vb[ok]) <= 1e-9 * np.maximum(np.abs(va[ok]), 1e-6))
+        assert np.all(np.abs(va[ok] - vb[ok]) <= 1e-9 * np.maximum(np.abs(va[ok]), floor))
 
 
 def test_rays_variable_length(mr, oracle, files):
