@@ -67,9 +67,9 @@ extern "C" {
  * Right-hand-side arithmetic of the plain FP64 kernel:
  *   MR_MATH_LIBM:     the reference's own calls (atan2, cos, sin, cosh, tanh,
  *                     sinh, three sqrt) in its own order.
- *   MR_MATH_IDENTITY: the same quantities from one expm1, one rsqrt and
- *                     kx/k, ky/k (exact identities; a few ulps apart), about
- *                     twice as fast on the FP64 pipe.
+ *   MR_MATH_IDENTITY: the same quantities from one expm1, one reciprocal,
+ *                     two rsqrt and kx/k, ky/k (exact identities, FMAs; a
+ *                     few ulps apart), about 4x as fast on the FP64 pipe.
  * Field lookups and interpolation are bit-identical to the reference in
  * both. */
 #define MR_STOP_STAGE1 0x0

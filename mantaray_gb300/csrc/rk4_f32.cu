@@ -19,9 +19,14 @@
 // keeps the offsets (and their rounding) small over tens of thousands of
 // steps.  FP64 is used only for that rebase and for the stored positions.
 //
+// Memory: each lane keeps the cell records it read last in registers and
+// reuses them while its ray stays in that cell; when the current is gridded
+// on the bathymetry's grid one cell lookup serves both fields.  The queue may
+// be taken in a spatial order (order.cu).
+//
 // Compiled with -fmad=false and every fused multiply-add written as fmaf, so
 // each ray's arithmetic is fixed by the source: results are bit-identical for
-// every launch shape (block size, blocks per SM, rays per lane).
+// every launch shape (block size, blocks per SM, rays per lane, ordering).
 
 #include <cuda_runtime.h>
 #include <math.h>
