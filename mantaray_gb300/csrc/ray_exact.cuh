@@ -13,7 +13,11 @@
 //      1 / (sinh a cosh a) = 4 q w,
 //    sqrt(g k tanh) and 1/sqrt(g k tanh) from one rsqrt, 1/k from another,
 //    and products and sums contracted into FMAs (kFma; the RK4 update too).
-//    Each quantity differs from the libm form by a few ulps.
+//    Each quantity differs from the libm form by a few ulps, except where
+//    exp(-2kh) falls below the rounding of 1 - exp(-2kh) (kh > ~18): q then
+//    comes out 0 (or a multiple of 2^-53) instead of its true value below
+//    1e-16, so the refraction term f ~ q is off by up to that amount -- a
+//    change of k below one ulp of kx, ky per step.
 // Both read the field values through the exact lookups, convert between f32
 // and f64 on the integer pipe (bits.h) and test NaN / zero on bit patterns,
 // which gives the same values as the conversion and comparison instructions.
