@@ -341,3 +341,20 @@ def test_seamount_full_size_properties(mr, oracle):
     oc = oracle.Current.grid(w.cx, w.cy, w.u, w.v)
     o = oracle.trace(ob, oc, w.x0[idx], w.y0[idx], w.kx0[idx], w.ky0[idx], w.t0, w.t_end, w.dt)
     H.assert_parity(np.ascontiguousarray(sub), rows1[idx], o[0], o[1], rtol=RTOL)
+
+
+def test_vortex_field_and_shelf_bump(mr, oracle):
+    # Smooth fields where every lookup matters: the multi-source case's
+    # generator (Gaussian shoals, 16 Gaussian vortices) at 512^2, and the
+    # differentiation case's shelf with its shoal and jet, 256 rays each,
+    # 2,000 steps, every row against the oracle.
+    from mantaray_gb300.workloads import multi_source, shelf_bump
+
+    scen, rays = multi_source(n_sources=8, rays_per_source=32, n_scenarios=1, n=512,
+                              steps=2000)
+    bx, by, depth, cx, cy, u, v = scen[0]
+    r = both(mr, oracle, ("grid", bx, by, depth), ("grid", cx, cy, u, v), rays["x0"],
+             rays["y0"], rays["kx0"], rays["ky0"], 0.0, 2000 * rays["dt"], rays["dt"])
+    check(*r)
+    w = shelf_bump(n_rays=256, steps=2000)
+    check(*_workload_both(mr, oracle, w))
