@@ -71,3 +71,14 @@ def gather_rays(local: np.ndarray, n_total: int, dst: int = 0):
         return None
     out = [p.cpu().numpy()[..., : b - a] for p, (a, b) in zip(parts, sizes)]
     return np.concatenate(out, axis=-1).astype(local.dtype, copy=False)
+
+
+def allreduce_node_gradients(*grads):
+    """Sums node-gradient arrays (torch tensors, e.g. the adjoint's depth, u
+    and v gradients of each rank's ray shard) over all ranks, in place: the
+    one exchange a sharded gradient needs (the per-ray work is independent,
+    the grid is shared).  Returns the tensors."""
+    dist = _dist()
+    for g in grads:
+        dist.all_reduce(g, op=dist.ReduceOp.SUM)
+    return grads

@@ -36,6 +36,12 @@ def _rank_main(rank, world, port, out_path):
         full_rows = D.gather_rays(rows.astype(np.float64)[None, :], w.n)
         t_max = D.reduce_scalar(float(rank + 1), "max")
         total = D.reduce_scalar(float(b - a), "sum")
+        # node gradients of each rank's shard summed over ranks (in place)
+        import torch
+
+        g = torch.full((3, 4), float(rank + 1), dtype=torch.float64)
+        D.allreduce_node_gradients(g)
+        assert bool((g == 3.0).all())
         if rank == 0:
             np.savez(out_path, traj=full, rows=full_rows, t_max=t_max, total=total)
         else:
