@@ -75,8 +75,8 @@ struct DiffArgs {
 // Fast math helpers per precision.
 __device__ __forceinline__ double t_expm1(double x) { return expm1(x); }
 __device__ __forceinline__ float t_expm1(float x) { return expm1f(x); }
-__device__ __forceinline__ double t_sqrt(double x) { return sqrt(x); }
-__device__ __forceinline__ float t_sqrt(float x) { return sqrtf(x); }
+__device__ __forceinline__ double t_rsqrt(double x) { return rsqrt(x); }
+__device__ __forceinline__ float t_rsqrt(float x) { return rsqrtf(x); }
 __device__ __forceinline__ double t_floor(double x) { return floor(x); }
 __device__ __forceinline__ float t_floor(float x) { return floorf(x); }
 
@@ -149,26 +149,36 @@ __device__ __forceinline__ bool eval(const DiffArgs<T> &A, const T s[4], Point<T
   const T k2 = s[2] * s[2] + s[3] * s[3];
   if (!(h > T(0)) || !(k2 > T(0))) return false;
   const T g = T(kG);
-  const T k = t_sqrt(k2);
+  // one expm1, one reciprocal and two rsqrt: m4 = 1 - exp(-4a) = m2 (2 - m2),
+  // w = 1 / m4, and 1/k, 1/sigma from rsqrt (exact identities)
+  const T rk = t_rsqrt(k2);
+  const T k = k2 * rk;
   P.k = k;
-  P.c = s[2] / k;
-  P.s = s[3] / k;
+  P.c = s[2] * rk;
+  P.s = s[3] * rk;
   const T a = k * h;
   const T m2 = -t_expm1(T(-2) * a);  // 1 - exp(-2a)
-  const T m4 = -t_expm1(T(-4) * a);  // 1 - exp(-4a)
   const T E = T(1) - m2;             // exp(-2a)
-  const T th = m2 / (T(2) - m2);     // tanh(a)
-  const T sech2 = T(4) * E / ((T(2) - m2) * (T(2) - m2));
-  const T isinh2 = T(2) * E / m4;    // 1/sinh(2a)
-  const T coth2 = (T(2) - m4) / m4;  // coth(2a)
-  const T sigma = t_sqrt(g * k * th);
+  const T p = T(2) - m2;             // 1 + exp(-2a)
+  const T m4 = m2 * p;               // 1 - exp(-4a)
+  const T w = T(1) / m4;
+  const T rp = m2 * w;               // 1 / p
+  const T th = m2 * rp;              // tanh(a)
+  const T sech2 = T(4) * E * rp * rp;
+  const T isinh2 = T(2) * E * w;     // 1/sinh(2a)
+  const T coth2 = (T(2) - m4) * w;   // coth(2a)
+  const T gkt = g * k * th;
+  const T rsig = t_rsqrt(gkt);
+  const T sigma = gkt * rsig;
+  const T hrsig = T(0.5) * rsig;     // 1 / (2 sigma)
+  const T hrk = T(0.5) * rk;         // 1 / (2 k)
   const T nfac = T(1) + T(2) * a * isinh2;
-  const T dsig_dk = g * (th + a * sech2) / (T(2) * sigma);
-  const T dsig_dh = g * k * k * sech2 / (T(2) * sigma);
+  const T dsig_dk = g * (th + a * sech2) * hrsig;
+  const T dsig_dh = g * k * k * sech2 * hrsig;
   const T dn_da = T(2) * isinh2 - T(4) * a * coth2 * isinh2;
-  P.q = sigma / (T(2) * k) * nfac;
-  P.q_k = dsig_dk / (T(2) * k) * nfac - sigma / (T(2) * k * k) * nfac + sigma / (T(2) * k) * dn_da * h;
-  P.q_h = dsig_dh / (T(2) * k) * nfac + sigma / (T(2) * k) * dn_da * k;
+  P.q = sigma * hrk * nfac;
+  P.q_k = hrk * ((dsig_dk - sigma * rk) * nfac + sigma * dn_da * h);
+  P.q_h = hrk * (dsig_dh * nfac + sigma * dn_da * k);
   P.f = -k * sigma * isinh2;
   P.f_k = -sigma * isinh2 - k * dsig_dk * isinh2 + T(2) * k * sigma * h * coth2 * isinh2;
   P.f_h = -k * dsig_dh * isinh2 + T(2) * k * k * sigma * coth2 * isinh2;
