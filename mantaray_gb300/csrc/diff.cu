@@ -130,7 +130,7 @@ template <typename T>
 struct Point {
   Cell<T> cb, cc;
   Interp<T> h, u, v;
-  T k, c, s;             // |k|, kx/k, ky/k
+  T k, rk, c, s;         // |k|, 1/|k|, kx/k, ky/k
   T q, q_k, q_h;         // group velocity and its partials
   T f, f_k, f_h;         // refraction factor and its partials
 };
@@ -154,6 +154,7 @@ __device__ __forceinline__ bool eval(const DiffArgs<T> &A, const T s[4], Point<T
   const T rk = t_rsqrt(k2);
   const T k = k2 * rk;
   P.k = k;
+  P.rk = rk;
   P.c = s[2] * rk;
   P.s = s[3] * rk;
   const T a = k * h;
@@ -236,8 +237,8 @@ __device__ __forceinline__ void jvp(const DiffArgs<T> &A, const T s[4], const Po
   const T du = P.u.dxp * ds[0] + P.u.dyp * ds[1] + dU;
   const T dv = P.v.dxp * ds[0] + P.v.dyp * ds[1] + dV;
   const T dk = P.c * ds[2] + P.s * ds[3];
-  const T dc = (P.s * P.s * ds[2] - P.c * P.s * ds[3]) / P.k;
-  const T dsn = (-P.c * P.s * ds[2] + P.c * P.c * ds[3]) / P.k;
+  const T dc = (P.s * P.s * ds[2] - P.c * P.s * ds[3]) * P.rk;
+  const T dsn = (-P.c * P.s * ds[2] + P.c * P.c * ds[3]) * P.rk;
   const T dq = P.q_k * dk + P.q_h * dh;
   const T df = P.f_k * dk + P.f_h * dh;
   dF[0] = dq * P.c + P.q * dc + du;
@@ -314,14 +315,15 @@ __device__ __forceinline__ void flush_current(const DiffArgs<T> &A, NodeAcc<T> &
 template <typename T>
 __device__ __forceinline__ void vjp(const DiffArgs<T> &A, const T s[4], const Point<T> &P,
                                     const T w[4], T r[4], NodeAcc<T> &acc) {
-  const T c = P.c, sn = P.s, k = P.k;
+  const T c = P.c, sn = P.s;
   const T g_h = (w[0] * c + w[1] * sn) * P.q_h + (w[2] * P.h.gx + w[3] * P.h.gy) * P.f_h;
   r[0] = P.h.dxp * g_h + w[0] * P.u.dxp + w[1] * P.v.dxp;
   r[1] = P.h.dyp * g_h + w[0] * P.u.dyp + w[1] * P.v.dyp;
-  const T cs_k = P.q * c * sn / k;
-  r[2] = w[0] * (P.q_k * c * c + P.q * sn * sn / k) + w[1] * (P.q_k * c * sn - cs_k) +
+  const T qrk = P.q * P.rk;
+  const T cs_k = qrk * c * sn;
+  r[2] = w[0] * (P.q_k * c * c + qrk * sn * sn) + w[1] * (P.q_k * c * sn - cs_k) +
          w[2] * (P.f_k * c * P.h.gx - P.u.gx) + w[3] * (P.f_k * c * P.h.gy - P.u.gy);
-  r[3] = w[0] * (P.q_k * sn * c - cs_k) + w[1] * (P.q_k * sn * sn + P.q * c * c / k) +
+  r[3] = w[0] * (P.q_k * sn * c - cs_k) + w[1] * (P.q_k * sn * sn + qrk * c * c) +
          w[2] * (P.f_k * sn * P.h.gx - P.v.gx) + w[3] * (P.f_k * sn * P.h.gy - P.v.gy);
   // bathymetry nodes of the cell
   {
