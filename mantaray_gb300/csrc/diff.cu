@@ -53,6 +53,7 @@ struct DGrid {
 template <typename T>
 struct DiffArgs {
   DGrid<T> bg, cg;
+  int same_grid;        // the current on the bathymetry's grid: one cell location serves both
   int64_t n;
   const T *x0, *y0, *kx0, *ky0;
   T dt;
@@ -141,7 +142,11 @@ constexpr double kG = 9.8;
 // (outside a grid, depth <= 0, k <= 0, non-finite).
 template <typename T>
 __device__ __forceinline__ bool eval(const DiffArgs<T> &A, const T s[4], Point<T> &P, T F[4]) {
-  if (!locate(A.bg, s[0], s[1], &P.cb) || !locate(A.cg, s[0], s[1], &P.cc)) return false;
+  if (!locate(A.bg, s[0], s[1], &P.cb)) return false;
+  if (A.same_grid)
+    P.cc = P.cb;
+  else if (!locate(A.cg, s[0], s[1], &P.cc))
+    return false;
   P.h = interp(A.bg.a, A.bg, P.cb);
   P.u = interp(A.cg.a, A.cg, P.cc);
   P.v = interp(A.cg.b, A.cg, P.cc);
@@ -548,6 +553,8 @@ int make_args(const mr_diff_grid *bgrid, const void *depth, const mr_diff_grid *
   A->cg = DGrid<T>{static_cast<const T *>(u), static_cast<const T *>(v), static_cast<int>(cgrid->nx),
                    static_cast<int>(cgrid->ny), T(cgrid->x0), T(cgrid->y0), T(1.0 / cgrid->dx),
                    T(1.0 / cgrid->dy)};
+  A->same_grid = bgrid->nx == cgrid->nx && bgrid->ny == cgrid->ny && bgrid->x0 == cgrid->x0 &&
+                 bgrid->y0 == cgrid->y0 && bgrid->dx == cgrid->dx && bgrid->dy == cgrid->dy;
   A->n = static_cast<int64_t>(n);
   A->x0 = static_cast<const T *>(x0);
   A->y0 = static_cast<const T *>(y0);
