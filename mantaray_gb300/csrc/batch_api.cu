@@ -184,6 +184,8 @@ int fill_args(mr_batch *b, size_t n, size_t n_stride, const uint8_t *ray_scenari
   int rc = check_config(cfg);
   if (rc) return rc;
   if (n > n_stride) return fail(MR_ERR_INVALID_ARGUMENT, "n exceeds the buffers' capacity");
+  if (cfg->order && n_stride > 0xffffffffull)
+    return fail(MR_ERR_INVALID_ARGUMENT, "ray ordering handles at most 2^32 - 1 rays per call");
   if (n_stride > 0 && (!x0 || !y0 || !kx0 || !ky0 || !end_state || !n_steps || !n_saved || !status))
     return fail(MR_ERR_INVALID_ARGUMENT, "null array argument");
   if (decimation < 0 || max_steps < 0 || max_steps >= INT32_MAX)
