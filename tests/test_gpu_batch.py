@@ -270,3 +270,39 @@ def test_pageable_host_outputs_are_refused(mr):
                       d.n_saved, d.status)
     with pytest.raises(MantarayError, match="page-locked"):
         tracer.trace(x0, y0, kx0, ky0, w.dt, 10, out=bad)
+
+
+def test_edge_rays_get_their_status(mr):
+    # NaN or outside starts, zero or infinite wavenumber, a dry start, and
+    # zero steps: every ray ends with the status that says why, none hangs
+    import torch
+
+    from mantaray_gb300 import _native as N
+    from mantaray_gb300.batch import BatchTracer
+
+    x, y, depth = H.bathymetry_arrays(100, 100, 100.0, 100.0,
+                                      lambda a, b: 50.0 if a < 5000.0 else -1.0)
+    cx, cy, u, v = H.current_arrays(100, 100, 100.0, 100.0, lambda a, b: (0.0, 0.0))
+    tracer = BatchTracer([(mr.Bathymetry.grid(x, y, depth),
+                           mr.Current.grid(cx.astype(np.float64), cy.astype(np.float64), u, v))])
+    nan, inf = float("nan"), float("inf")
+    x0 = [1000.0, nan, -500.0, 1000.0, 1000.0, 7000.0]
+    kx0 = [0.01, 0.01, 0.01, 0.0, inf, 0.01]
+    rays = _dev(np.array(x0), np.full(6, 4000.0), np.array(kx0), np.zeros(6))
+    res = tracer.trace(*rays, 1.0, 50)
+    torch.cuda.synchronize()
+    st = res.status.cpu().numpy().tolist()
+    assert st == [N.BATCH_COMPLETE, N.BATCH_OUT_OF_DOMAIN, N.BATCH_OUT_OF_DOMAIN,
+                  N.BATCH_BAD_WAVENUMBER, N.BATCH_BAD_WAVENUMBER, N.BATCH_DRY], st
+    assert res.n_steps.cpu().numpy().tolist() == [50, 0, 0, 0, 0, 0]
+    # zero steps: every ray complete where it started
+    res0 = tracer.trace(*rays, 1.0, 0)
+    torch.cuda.synchronize()
+    end = res0.end_state.cpu().numpy()
+    assert res0.n_steps.cpu().numpy().tolist() == [0] * 6
+    np.testing.assert_array_equal(end[1, [0, 2, 3, 5]], np.array(x0)[[0, 2, 3, 5]])
+    # no rays at all
+    empty = [t[:0] for t in rays]
+    out = tracer.trace(*empty, 1.0, 10)
+    torch.cuda.synchronize()
+    assert out.n_steps.numel() == 0
