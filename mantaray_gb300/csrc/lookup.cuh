@@ -12,6 +12,8 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "fields.h"
 
 namespace mr {
@@ -123,6 +125,72 @@ __device__ __forceinline__ int bilinear_cell(float ax1, float ax2, float ay1, fl
   return RHS_OK;
 }
 
+// What bilinear_cell computes from a regular cell alone, kept so that the
+// next lookups in the same cell skip the loads and the two divisions: corner
+// coordinates, the inverse's entries and each value set's coefficients.
+// x1 == kNoCell: empty.
+constexpr uint32_t kNoCell = 0xffffffffu;
+template <int NV>
+struct CellWeights {
+  uint32_t x1 = kNoCell, y1 = kNoCell;
+  float ax1, ax2, ay1, ay2;
+  float m00, m01, m10;
+  float a00[NV], a10[NV], a01[NV], a11[NV];
+};
+
+// Fills W when bilinear_cell's fast path applies to the corners (finite
+// coordinates and edges, det != 0); false otherwise.
+template <int NV>
+__device__ __forceinline__ bool cell_prepare(float ax1, float ax2, float ay1, float ay2,
+                                             const float (&pv)[NV][4], CellWeights<NV> &W) {
+  const float bt1 = __fsub_rn(ay2, ay1);
+  const float dt0 = __fsub_rn(ax2, ax1);
+  if (!(isfinite(ax1) && isfinite(ay1) && isfinite(bt1) && isfinite(dt0))) return false;
+  const float det = __fsub_rn(0.0f, __fmul_rn(dt0, bt1));
+  if (det == 0.0f) return false;
+  W.ax1 = ax1; W.ax2 = ax2; W.ay1 = ay1; W.ay2 = ay2;
+  W.m00 = det > 0.0f ? 0.0f : -0.0f;
+  W.m01 = -__fdiv_rn(dt0, det);
+  W.m10 = -__fdiv_rn(bt1, det);
+#pragma unroll
+  for (int v = 0; v < NV; ++v) {
+    W.a00[v] = pv[v][0];
+    W.a10[v] = __fsub_rn(pv[v][1], pv[v][0]);
+    W.a01[v] = __fsub_rn(pv[v][3], pv[v][0]);
+    W.a11[v] = __fsub_rn(__fsub_rn(__fsub_rn(pv[v][2], pv[v][0]), W.a10[v]), W.a01[v]);
+  }
+  return true;
+}
+
+// bilinear_cell from prepared weights, the same operations in the same
+// order; false when the target is a corner (the full path returns it).
+template <int NV>
+__device__ __forceinline__ bool cell_apply(const CellWeights<NV> &W, float tx, float ty,
+                                           float (&out)[NV]) {
+  if ((tx == W.ax1 || tx == W.ax2) && (ty == W.ay1 || ty == W.ay2)) return false;
+  const float tt0 = __fsub_rn(tx, W.ax1), tt1 = __fsub_rn(ty, W.ay1);
+  const float x = __fadd_rn(__fmul_rn(W.m00, tt0), __fmul_rn(W.m01, tt1));
+  const float y = __fadd_rn(__fmul_rn(W.m10, tt0), __fmul_rn(W.m00, tt1));
+#pragma unroll
+  for (int v = 0; v < NV; ++v)
+    out[v] = __fadd_rn(__fadd_rn(__fadd_rn(W.a00[v], __fmul_rn(W.a10[v], x)),
+                                 __fmul_rn(W.a01[v], y)),
+                       __fmul_rn(__fmul_rn(W.a11[v], x), y));
+  return true;
+}
+
+// Lookup caches: NoCache does nothing; LookupCache keeps the cells a lane
+// looked up last (bathymetry and current) for the next lookups in them.  On
+// a hit the loads and divisions that depend on the cell alone are skipped:
+// shorter dependent chains for calls too small to hide them; for large
+// calls the FP64 pipe bounds the plain kernel and the extra registers do not
+// pay, so the kernel takes NoCache there.
+struct NoCache {};
+struct LookupCache {
+  CellWeights<1> b;
+  CellWeights<2> c;
+};
+
 // nearest + the edge/on-grid/interior corner rule (cartesian_netcdf3.rs:274-390
 // in f32, cartesian_current.rs:231-339 in f64).  a0/sp/high are the host
 // precomputed a[0], |a[1]-a[0]| and (n-1) as T; n >= 2.
@@ -208,8 +276,10 @@ __device__ __forceinline__ int corner_pair_thr(double target, float target32, fl
 }
 
 // BathymetryData::depth_and_gradient for every kind.  out = (h, dh/dx, dh/dy).
+template <typename Cache = NoCache>
 __device__ __forceinline__ int depth_and_gradient(const BathyDev &b, float x, float y,
-                                                  float out[3]) {
+                                                  float out[3], Cache *L = nullptr) {
+  constexpr bool kCache = std::is_same<Cache, LookupCache>::value;
   if (b.kind == BATHY_GRID) {
     // cartesian_netcdf3.rs:98-135
     if (isnan(x) || isnan(y)) {
@@ -221,10 +291,21 @@ __device__ __forceinline__ int depth_and_gradient(const BathyDev &b, float x, fl
     if (e) return e;
     e = corner_pair<float>(y, b.y0, b.ysp, b.yhigh, &y1, &y2);
     if (e) return e;
+    const bool regular = x2 == x1 + 1 && y2 == y1 + 1;
+    float depth[1];
+    if constexpr (kCache) {
+      if (regular && x1 == L->b.x1 && y1 == L->b.y1 && cell_apply<1>(L->b, x, y, depth)) {
+        const uint64_t sw = b.nx * y1 + x1;
+        out[0] = depth[0];
+        out[1] = __ldg(b.gx + sw);
+        out[2] = __ldg(b.gy + sw);
+        return RHS_OK;
+      }
+    }
     // depth_at_indexes checks every corner's flat index against the array
     // length (:465-471); the largest of them is nx*y2 + x2.
     uint64_t sw, nw, ne, se;
-    if (x2 == x1 + 1 && y2 == y1 + 1) {
+    if (regular) {
       sw = b.nx * y1 + x1; nw = sw + b.nx; se = sw + 1; ne = nw + 1;
     } else {
       sw = b.nx * y1 + x1; nw = b.nx * y2 + x1; ne = b.nx * y2 + x2; se = b.nx * y1 + x2;
@@ -232,14 +313,20 @@ __device__ __forceinline__ int depth_and_gradient(const BathyDev &b, float x, fl
     if (ne >= b.depth_len) return RHS_INDEX_OUT_OF_BOUNDS;
     const float pv[1][4] = {{__ldg(b.depth32 + sw), __ldg(b.depth32 + nw),
                              __ldg(b.depth32 + ne), __ldg(b.depth32 + se)}};
-    float depth[1];
-    e = bilinear_cell<1>(__ldg(b.x + x1), __ldg(b.x + x2), __ldg(b.y + y1), __ldg(b.y + y2), pv,
-                         x, y, depth);
+    const float ax1 = __ldg(b.x + x1), ax2 = __ldg(b.x + x2);
+    const float ay1 = __ldg(b.y + y1), ay2 = __ldg(b.y + y2);
+    e = bilinear_cell<1>(ax1, ax2, ay1, ay2, pv, x, y, depth);
     if (e) return e;
     out[0] = depth[0];
-    if (x2 == x1 + 1 && y2 == y1 + 1) {
+    if (regular) {
       out[1] = __ldg(b.gx + sw);
       out[2] = __ldg(b.gy + sw);
+      if constexpr (kCache) {
+        if (x1 < kNoCell && y1 < kNoCell && cell_prepare<1>(ax1, ax2, ay1, ay2, pv, L->b)) {
+          L->b.x1 = static_cast<uint32_t>(x1);
+          L->b.y1 = static_cast<uint32_t>(y1);
+        }
+      }
     } else {  // degenerate corners (NaN index): the reference's own expression
       const double d_sw = __ldg(b.depth + sw);
       out[1] = __double2float_rn((__ldg(b.depth + se) - d_sw) / b.xspace);
@@ -276,8 +363,10 @@ __device__ __forceinline__ int depth_and_gradient(const BathyDev &b, float x, fl
 }
 
 // CurrentData::current_and_gradient.  out = (u, v, du/dx, du/dy, dv/dx, dv/dy).
+template <typename Cache = NoCache>
 __device__ __forceinline__ int current_and_gradient(const CurrentDev &c, double x, double y,
-                                                    double out[6]) {
+                                                    double out[6], Cache *L = nullptr) {
+  constexpr bool kCache = std::is_same<Cache, LookupCache>::value;
   if (c.kind == CURRENT_CONSTANT) {
     out[0] = c.cu; out[1] = c.cv;
     out[2] = out[3] = out[4] = out[5] = 0.0;
@@ -294,8 +383,22 @@ __device__ __forceinline__ int current_and_gradient(const CurrentDev &c, double 
   if (c.ythr) e = corner_pair_thr(y, ty, c.y0f, c.inv_yspf, c.ythr, c.ny, &y1, &y2);
   if (e < 0) e = corner_pair_f64(y, c.y0, c.ysp, c.inv_ysp, c.yhigh, &y1, &y2);
   if (e) return e;
+  const bool regular = x2 == x1 + 1 && y2 == y1 + 1;
+  float uv[2];
+  if constexpr (kCache) {
+    if (regular && x1 == L->c.x1 && y1 == L->c.y1 && cell_apply<2>(L->c, tx, ty, uv)) {
+      const uint64_t sw = c.nx * y1 + x1;
+      out[0] = f2d(uv[0]);
+      out[1] = f2d(uv[1]);
+      out[2] = __ldg(c.dudx + sw);
+      out[3] = __ldg(c.dudy + sw);
+      out[4] = __ldg(c.dvdx + sw);
+      out[5] = __ldg(c.dvdy + sw);
+      return RHS_OK;
+    }
+  }
   uint64_t sw, nw, ne, se;
-  if (x2 == x1 + 1 && y2 == y1 + 1) {
+  if (regular) {
     sw = c.nx * y1 + x1; nw = sw + c.nx; se = sw + 1; ne = nw + 1;
   } else {
     sw = c.nx * y1 + x1; nw = c.nx * y2 + x1; ne = c.nx * y2 + x2; se = c.nx * y1 + x2;
@@ -305,18 +408,22 @@ __device__ __forceinline__ int current_and_gradient(const CurrentDev &c, double 
   const float pv[2][4] = {
       {__ldg(c.u32 + sw), __ldg(c.u32 + nw), __ldg(c.u32 + ne), __ldg(c.u32 + se)},
       {__ldg(c.v32 + sw), __ldg(c.v32 + nw), __ldg(c.v32 + ne), __ldg(c.v32 + se)}};
-  float uv[2];
-  if ((e = bilinear_cell<2>(__ldg(c.x32 + x1), __ldg(c.x32 + x2), __ldg(c.y32 + y1),
-                            __ldg(c.y32 + y2), pv, tx, ty, uv)))
-    return e;
-  const float u = uv[0], v = uv[1];
-  out[0] = f2d(u);
-  out[1] = f2d(v);
-  if (x2 == x1 + 1 && y2 == y1 + 1) {
+  const float ax1 = __ldg(c.x32 + x1), ax2 = __ldg(c.x32 + x2);
+  const float ay1 = __ldg(c.y32 + y1), ay2 = __ldg(c.y32 + y2);
+  if ((e = bilinear_cell<2>(ax1, ax2, ay1, ay2, pv, tx, ty, uv))) return e;
+  out[0] = f2d(uv[0]);
+  out[1] = f2d(uv[1]);
+  if (regular) {
     out[2] = __ldg(c.dudx + sw);
     out[3] = __ldg(c.dudy + sw);
     out[4] = __ldg(c.dvdx + sw);
     out[5] = __ldg(c.dvdy + sw);
+    if constexpr (kCache) {
+      if (x1 < kNoCell && y1 < kNoCell && cell_prepare<2>(ax1, ax2, ay1, ay2, pv, L->c)) {
+        L->c.x1 = static_cast<uint32_t>(x1);
+        L->c.y1 = static_cast<uint32_t>(y1);
+      }
+    }
   } else {
     const double u_sw = __ldg(c.u + sw), v_sw = __ldg(c.v + sw);
     out[2] = (__ldg(c.u + se) - u_sw) / c.xspace;

@@ -37,16 +37,18 @@ struct RhsLibm {
   static constexpr bool kFma = false;
   // WaveRayPath::odes with group_velocity (:177-188) and dkdt_bathy
   // (:207-216) inlined in the reference's order.
+  template <typename Cache>
   __device__ __forceinline__ static int odes(const BathyDev &b, const CurrentDev &c, double x,
-                                             double y, double kx, double ky, double out[4]) {
+                                             double y, double kx, double ky, double out[4],
+                                             Cache *L) {
     float hg[3];
-    int e = depth_and_gradient(b, d2f(x), d2f(y), hg);
+    int e = depth_and_gradient<Cache>(b, d2f(x), d2f(y), hg, L);
     if (e) return e;
     const double h = f2d(hg[0]);
     const double dhdx = f2d(hg[1]);
     const double dhdy = f2d(hg[2]);
     double cur[6];
-    e = current_and_gradient(c, x, y, cur);
+    e = current_and_gradient<Cache>(c, x, y, cur, L);
     if (e) return e;
     const double k = sqrt(kx * kx + ky * ky);
     const double theta = atan2(ky, kx);
@@ -74,13 +76,15 @@ struct RhsLibm {
 
 struct RhsIdentity {
   static constexpr bool kFma = true;
+  template <typename Cache>
   __device__ __forceinline__ static int odes(const BathyDev &b, const CurrentDev &c, double x,
-                                             double y, double kx, double ky, double out[4]) {
+                                             double y, double kx, double ky, double out[4],
+                                             Cache *L) {
     float hg[3];
-    int e = depth_and_gradient(b, d2f(x), d2f(y), hg);
+    int e = depth_and_gradient<Cache>(b, d2f(x), d2f(y), hg, L);
     if (e) return e;
     double cur[6];
-    e = current_and_gradient(c, x, y, cur);
+    e = current_and_gradient<Cache>(c, x, y, cur, L);
     if (e) return e;
     const double h = f2d(hg[0]);
     const double k2 = fma(kx, kx, ky * ky);
@@ -109,10 +113,11 @@ struct RhsIdentity {
 };
 
 // impl System::system (src/wave_ray_path.rs:220-234): errors become NaN.
-template <typename Rhs>
+// Cache: NoCache, or LookupCache with the lane's last cells (lookup.cuh).
+template <typename Rhs, typename Cache = NoCache>
 __device__ __forceinline__ void system(const BathyDev &b, const CurrentDev &c, const double s[4],
-                                       double ds[4]) {
-  if (Rhs::odes(b, c, s[0], s[1], s[2], s[3], ds) != RHS_OK) {
+                                       double ds[4], Cache *L = nullptr) {
+  if (Rhs::odes(b, c, s[0], s[1], s[2], s[3], ds, L) != RHS_OK) {
     ds[0] = ds[1] = ds[2] = ds[3] = f64_nan();
   }
 }

@@ -341,6 +341,13 @@ def test_seamount_full_size_properties(mr, oracle):
     oc = oracle.Current.grid(w.cx, w.cy, w.u, w.v)
     o = oracle.trace(ob, oc, w.x0[idx], w.y0[idx], w.kx0[idx], w.ky0[idx], w.t0, w.t_end, w.dt)
     H.assert_parity(np.ascontiguousarray(sub), rows1[idx], o[0], o[1], rtol=RTOL)
+    # The same rays traced alone (a small call: the kernel keeps each lane's
+    # last cells, which a full-size call does not) give the same bits.
+    del traj
+    small = mr.trace(b, c, w.x0[idx], w.y0[idx], w.kx0[idx], w.ky0[idx], w.t_end - w.t0, w.dt,
+                     t0=w.t0, math=MATH)
+    assert np.array_equal(small.n_rows, rows1[idx])
+    assert np.array_equal(np.nan_to_num(small.traj, nan=-1e300), np.nan_to_num(sub, nan=-1e300))
 
 
 def test_vortex_field_and_shelf_bump(mr, oracle):
