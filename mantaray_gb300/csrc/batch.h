@@ -51,6 +51,7 @@ struct BatchArgs {
   int64_t n;                 // rays of this call
   const double *x0, *y0, *kx0, *ky0;  // [n] initial states
   double t0, dt;
+  float dt_f, half_f, sixth_f;  // (float)dt, dt/2, dt/6 as the integrator uses them
   int64_t max_steps;
   int64_t decimation;        // store every `decimation`-th step (0: endpoints only)
   int64_t save_cap;          // rows of `saved` per ray

@@ -204,6 +204,9 @@ int fill_args(mr_batch *b, size_t n, size_t n_stride, const uint8_t *ray_scenari
   a->x0 = x0; a->y0 = y0; a->kx0 = kx0; a->ky0 = ky0;
   a->t0 = t0;
   a->dt = dt;
+  a->dt_f = static_cast<float>(dt);
+  a->half_f = 0.5f * a->dt_f;
+  a->sixth_f = a->dt_f * (1.0f / 6.0f);
   a->max_steps = max_steps;
   a->decimation = decimation;
   a->save_cap = static_cast<int64_t>(save_cap);
@@ -379,6 +382,9 @@ int mr_batch_graph_create(mr_batch *b, size_t n_max, const uint8_t *ray_scenario
     gr->oargs = order_args(b, a, gr->ord);
   }
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  // the integrator build for this shape, chosen (an occupancy query) before
+  // the capture begins
+  (void)mr::rk4_f32_function(cfg->rays_per_lane, cfg->block, cfg->blocks_per_sm);
   if (e == cudaSuccess) e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
     cudaError_t le = enqueue(b, a, cfg, &gr->ord, s);
@@ -400,7 +406,8 @@ int mr_batch_graph_create(mr_batch *b, size_t n_max, const uint8_t *ray_scenario
       if (p.func == mr::order_keys_function()) {
         gr->order_node = nodes[i];
         gr->order_params = p;
-      } else if (p.func == mr::rk4_f32_function(cfg->rays_per_lane)) {
+      } else if (p.func == mr::rk4_f32_function(cfg->rays_per_lane, cfg->block,
+                                                cfg->blocks_per_sm)) {
         gr->kernel_node = nodes[i];
         gr->params = p;
       }

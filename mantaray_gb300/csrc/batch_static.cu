@@ -110,6 +110,9 @@ extern "C" int mr_batch_trace_device_static(
   a.x0 = x0; a.y0 = y0; a.kx0 = kx0; a.ky0 = ky0;
   a.t0 = t0;
   a.dt = dt;
+  a.dt_f = static_cast<float>(dt);
+  a.half_f = 0.5f * a.dt_f;
+  a.sixth_f = a.dt_f * (1.0f / 6.0f);
   a.max_steps = max_steps;
   a.decimation = decimation;
   a.save_cap = static_cast<int64_t>(save_cap);

@@ -32,6 +32,8 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #include "batch.h"
 #include "fields.h"
 #include "kernels.h"
@@ -211,14 +213,15 @@ __device__ __forceinline__ int rhs_f32(const ScenarioDev &s, RayLane &L, float p
   const float inv_d = __frcp_rn(m * (2.0f - m));  // = 1.0f / x, correctly rounded
   const float r = m * inv_d;            // 1 / (2 - m)
   const float th = m * r;               // tanh(kh)
-  const float kh_ch2 = 4.0f * kh * q * r * r;
-  const float inv_shch = 4.0f * q * (2.0f - m) * inv_d * r;
   const float gkt = kGf * k * th;
   const float rs = rsqrtf(gkt);
-  const float cg = 0.5f * kGf * (th + kh_ch2) * rs;
-  const float f = -0.5f * k * inv_shch * (gkt * rs);
-  d[0] = fmaf(cg, kx * rk, u);
-  d[1] = fmaf(cg, ky * rk, v);
+  const float q4 = 4.0f * q;
+  // kh / cosh^2(kh) = 4 kh q r^2 and 1 / (sinh(kh) cosh(kh)) = 4 q inv_d
+  const float cg = (0.5f * kGf) * (fmaf(kh * q4, r * r, th) * rs);
+  const float f = (-0.5f * k) * ((q4 * inv_d) * (gkt * rs));
+  const float cgk = cg * rk;            // c_g / k: c_g cos(theta) = cgk kx
+  d[0] = fmaf(cgk, kx, u);
+  d[1] = fmaf(cgk, ky, v);
   d[2] = fmaf(-ky, dvdx, fmaf(-kx, dudx, f * C.bx));
   d[3] = fmaf(-ky, dvdy, fmaf(-kx, dudy, f * C.by));
   return BATCH_COMPLETE;
@@ -295,8 +298,10 @@ __device__ __forceinline__ void start(const BatchArgs &a, RayLane &L, int64_t r)
 // One RK4 step of lane L.  Returns BATCH_COMPLETE while the ray goes on.
 __device__ __forceinline__ int advance(const BatchArgs &a, RayLane &L) {
   const ScenarioDev &s = a.scen[L.scen];
-  const float dt = static_cast<float>(a.dt);
-  const float half = 0.5f * dt;
+  // step constants in FP32 from the host (a conversion here would run on the
+  // FP64 pipe, and the compiler re-derives such values under register pressure)
+  const float dt = a.dt_f;
+  const float half = a.half_f;
   float k1[4], k2[4], k3[4], k4[4];
   int st = rhs_f32(s, L, L.px, L.py, L.kx, L.ky, k1);
   if (st == BATCH_COMPLETE)
@@ -309,7 +314,7 @@ __device__ __forceinline__ int advance(const BatchArgs &a, RayLane &L) {
     st = rhs_f32(s, L, fmaf(dt, k3[0], L.px), fmaf(dt, k3[1], L.py), fmaf(dt, k3[2], L.kx),
                  fmaf(dt, k3[3], L.ky), k4);
   if (st != BATCH_COMPLETE) return st;
-  const float sixth = dt * (1.0f / 6.0f);
+  const float sixth = a.sixth_f;
 #pragma unroll
   for (int q = 0; q < 4; ++q) k1[q] = sixth * fmaf(2.0f, k2[q] + k3[q], k1[q] + k4[q]);
   kahan_add(L.px, L.cpx, k1[0]);
@@ -330,7 +335,7 @@ __device__ __forceinline__ int advance(const BatchArgs &a, RayLane &L) {
 }
 
 template <int RPT>
-__global__ void __launch_bounds__(256) rk4_f32_kernel(BatchArgs a) {
+__device__ __forceinline__ void k2_body(const BatchArgs &a) {
   const int lane = threadIdx.x & 31;
   const unsigned lt_mask = (1u << lane) - 1u;
   const int64_t n = a.n;
@@ -371,6 +376,22 @@ __global__ void __launch_bounds__(256) rk4_f32_kernel(BatchArgs a) {
   }
 }
 
+// One ray per lane, two builds.  rk4_f32_kernel_1 takes the compiler's
+// register count (~100: 4 blocks of 128 threads, 16 warps, per SM).
+// rk4_f32_kernel_1r is capped at 72 registers (28 warps per SM; 80 B
+// spilled to L1).  The kernel is issue- and latency-bound; when a call has
+// rays for more warps than the first keeps resident, the extra warps hide
+// more of the dependent FP32 chains than the spills cost (4,096^2
+// shelf-slope, 2^20 rays: 30.6 -> 32.7 G ray-steps/s at 128 x 8; caps of
+// 80 / 64 / 56 registers gave 32.0 / 32.7 / 31.5); with fewer rays than
+// lanes the spills only add latency (65,536-ray seamount: 22.2 -> 19.3).
+// The launcher takes the capped build when the launch asks for more blocks
+// per SM than the uncapped one holds.
+__global__ void __launch_bounds__(256) rk4_f32_kernel_1(BatchArgs a) { k2_body<1>(a); }
+__global__ void __maxnreg__(72) rk4_f32_kernel_1r(BatchArgs a) { k2_body<1>(a); }
+// Two rays per lane hold twice the lane state: no cap.
+__global__ void __launch_bounds__(256) rk4_f32_kernel_2(BatchArgs a) { k2_body<2>(a); }
+
 }  // namespace
 
 cudaError_t launch_pack_bathy(const BathyDev &b, float4 *cells, cudaStream_t stream) {
@@ -410,6 +431,28 @@ cudaError_t launch_fill_nan(float *p, int64_t count, cudaStream_t stream) {
   return cudaGetLastError();
 }
 
+// Resident blocks per SM of rk4_f32_kernel_1 by block size (multiples of 32
+// up to 256), queried once; 0: not yet known.
+static std::atomic<int> g_resident_1[9];
+
+const void *rk4_f32_function(int rays_per_lane, int block, int blocks_per_sm) {
+  if (rays_per_lane == 2) return reinterpret_cast<const void *>(&rk4_f32_kernel_2);
+  const int slot = (block >= 32 && block <= 256 && block % 32 == 0) ? block / 32 : 0;
+  int resident = slot ? g_resident_1[slot].load(std::memory_order_relaxed) : 0;
+  if (resident == 0) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, rk4_f32_kernel_1, block, 0) !=
+            cudaSuccess ||
+        resident < 1) {
+      (void)cudaGetLastError();
+      resident = blocks_per_sm;  // unknown: the uncapped build
+    } else if (slot) {
+      g_resident_1[slot].store(resident, std::memory_order_relaxed);
+    }
+  }
+  return resident < blocks_per_sm ? reinterpret_cast<const void *>(&rk4_f32_kernel_1r)
+                                  : reinterpret_cast<const void *>(&rk4_f32_kernel_1);
+}
+
 cudaError_t launch_rk4_f32(const BatchArgs &a, int block, int blocks_per_sm, int rays_per_lane,
                            cudaStream_t stream) {
   int dev = 0, sms = 0;
@@ -418,16 +461,9 @@ cudaError_t launch_rk4_f32(const BatchArgs &a, int block, int blocks_per_sm, int
   e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess) return e;
   const unsigned grid = static_cast<unsigned>(sms * blocks_per_sm);
-  if (rays_per_lane == 2)
-    rk4_f32_kernel<2><<<grid, block, 0, stream>>>(a);
-  else
-    rk4_f32_kernel<1><<<grid, block, 0, stream>>>(a);
-  return cudaGetLastError();
-}
-
-const void *rk4_f32_function(int rays_per_lane) {
-  return rays_per_lane == 2 ? reinterpret_cast<const void *>(&rk4_f32_kernel<2>)
-                            : reinterpret_cast<const void *>(&rk4_f32_kernel<1>);
+  void *args[] = {const_cast<BatchArgs *>(&a)};
+  return cudaLaunchKernel(rk4_f32_function(rays_per_lane, block, blocks_per_sm), dim3(grid),
+                          dim3(block), args, 0, stream);
 }
 
 }  // namespace mr
