@@ -3,8 +3,9 @@
 // K5 (pack_*_cells): repacks a bathymetry / current grid of the plain form
 // (f64 values in HBM) into the cell records of batch.h, one thread per cell.
 //
-// K2 (rk4_f32_kernel): a persistent kernel, grid = SMs x resident blocks.
-// Each lane holds RAYS_PER_LANE rays.  A lane whose ray has ended refills from
+// K2 (rk4_f32_kernel_1 / _1r / _2): a persistent kernel, grid = SMs x
+// blocks per SM.  Each lane holds 1 or 2 rays (_2); one ray per lane has an
+// uncapped and a 72-register build (_1r), chosen by the launch shape.  A lane whose ray has ended refills from
 // a device work queue: the warp ballots its empty slots, one lane reserves
 // that many ray indices with a single atomicAdd and the indices are handed out
 // by rank within the ballot, so lanes never idle while work remains and rays
@@ -26,7 +27,8 @@
 //
 // Compiled with -fmad=false and every fused multiply-add written as fmaf, so
 // each ray's arithmetic is fixed by the source: results are bit-identical for
-// every launch shape (block size, blocks per SM, rays per lane, ordering).
+// every launch shape (block size, blocks per SM, rays per lane, ordering)
+// and both register builds.
 
 #include <cuda_runtime.h>
 #include <math.h>
