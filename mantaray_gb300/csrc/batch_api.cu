@@ -56,6 +56,8 @@ int pack_bathy(mr_batch *b, const mr_bathymetry *h, mr::PackedGrid *g, cudaStrea
   g->sp_y = h->dev.yspace;
   g->inv_sp_x = static_cast<float>(1.0 / h->dev.xspace);
   g->inv_sp_y = static_cast<float>(1.0 / h->dev.yspace);
+  g->cx_max = static_cast<float>(g->nx - 2);
+  g->cy_max = static_cast<float>(g->ny - 2);
   g->inv_sp_xd = 1.0 / h->dev.xspace;
   g->inv_sp_yd = 1.0 / h->dev.yspace;
   g->kind = 0;
@@ -72,6 +74,7 @@ int pack_current(mr_batch *b, const mr_current *c, mr::PackedGrid *g, cudaStream
     g->x0 = g->y0 = 0.0;
     g->sp_x = g->sp_y = 1.0;
     g->inv_sp_x = g->inv_sp_y = 1.0f;
+    g->cx_max = g->cy_max = 0.0f;
     g->inv_sp_xd = g->inv_sp_yd = 1.0;
     return MR_OK;
   }
@@ -92,6 +95,8 @@ int pack_current(mr_batch *b, const mr_current *c, mr::PackedGrid *g, cudaStream
   g->sp_y = c->dev.yspace;
   g->inv_sp_x = static_cast<float>(1.0 / c->dev.xspace);
   g->inv_sp_y = static_cast<float>(1.0 / c->dev.yspace);
+  g->cx_max = static_cast<float>(g->nx - 2);
+  g->cy_max = static_cast<float>(g->ny - 2);
   g->inv_sp_xd = 1.0 / c->dev.xspace;
   g->inv_sp_yd = 1.0 / c->dev.yspace;
   g->kind = 0;
@@ -198,6 +203,7 @@ int fill_args(mr_batch *b, size_t n, size_t n_stride, const uint8_t *ray_scenari
   }
   if (!(dt > 0.0) || !isfinite(t0)) return fail(MR_ERR_INVALID_ARGUMENT, "dt must be > 0");
   a->scen = b->scen;
+  a->scen0 = b->host_scen[0];
   a->n_scenarios = b->n_scenarios;
   a->ray_scenario = ray_scenario;
   a->n = static_cast<int64_t>(n);
@@ -384,7 +390,8 @@ int mr_batch_graph_create(mr_batch *b, size_t n_max, const uint8_t *ray_scenario
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
   // the integrator build for this shape, chosen (an occupancy query) before
   // the capture begins
-  (void)mr::rk4_f32_function(cfg->rays_per_lane, cfg->block, cfg->blocks_per_sm);
+  (void)mr::rk4_f32_function(cfg->rays_per_lane, cfg->block, cfg->blocks_per_sm,
+                             b->n_scenarios);
   if (e == cudaSuccess) e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
     cudaError_t le = enqueue(b, a, cfg, &gr->ord, s);
@@ -407,7 +414,7 @@ int mr_batch_graph_create(mr_batch *b, size_t n_max, const uint8_t *ray_scenario
         gr->order_node = nodes[i];
         gr->order_params = p;
       } else if (p.func == mr::rk4_f32_function(cfg->rays_per_lane, cfg->block,
-                                                cfg->blocks_per_sm)) {
+                                                cfg->blocks_per_sm, b->n_scenarios)) {
         gr->kernel_node = nodes[i];
         gr->params = p;
       }

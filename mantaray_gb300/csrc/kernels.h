@@ -33,9 +33,9 @@ cudaError_t launch_pack_bathy(const BathyDev &b, float4 *cells, cudaStream_t str
 cudaError_t launch_pack_current(const CurrentDev &c, float4 *cells, cudaStream_t stream);
 cudaError_t launch_rk4_f32(const BatchArgs &a, int block, int blocks_per_sm, int rays_per_lane,
                            cudaStream_t stream);
-// The integrator build a launch of this shape runs (a graph's kernel node
-// is found by it).
-const void *rk4_f32_function(int rays_per_lane, int block, int blocks_per_sm);
+// The integrator build a launch of this shape and scenario count runs (a
+// graph's kernel node is found by it).
+const void *rk4_f32_function(int rays_per_lane, int block, int blocks_per_sm, int n_scenarios);
 cudaError_t launch_fill_nan(float *p, int64_t count, cudaStream_t stream);
 
 // Spatial ordering of a batched call's rays (K6): sorts by key in `passes`

@@ -100,10 +100,11 @@ __global__ void pack_current_cells(CurrentDev cu, float4 *cells) {
 constexpr unsigned kFull = 0xffffffffu;
 constexpr float kGf = 9.8f;
 
-// Position of a lane on one grid: integer cell base of its origin plus the
-// origin's fractional cell offset.
+// Position of a lane on one grid: the cell of its origin (integral floats:
+// exact, grids have fewer than 2^24 points per axis) plus the origin's
+// fractional cell offset.
 struct GridPos {
-  int i0, j0;
+  float fi0, fj0;
   float f0, g0;
 };
 
@@ -111,29 +112,27 @@ __device__ __forceinline__ GridPos grid_pos(const PackedGrid &g, double ox, doub
   GridPos p;
   const double ux = (ox - g.x0) * g.inv_sp_xd, uy = (oy - g.y0) * g.inv_sp_yd;
   const double fx = floor(ux), fy = floor(uy);
-  // clamp far-away origins so the int conversion stays defined; such a lane
-  // fails the in-range test of its first lookup
-  p.i0 = static_cast<int>(fmin(fmax(fx, -1.0e9), 1.0e9));
-  p.j0 = static_cast<int>(fmin(fmax(fy, -1.0e9), 1.0e9));
+  // clamp far-away origins (+-1e9 is exact in FP32); such a lane fails the
+  // in-range test of its first lookup
+  p.fi0 = static_cast<float>(fmin(fmax(fx, -1.0e9), 1.0e9));
+  p.fj0 = static_cast<float>(fmin(fmax(fy, -1.0e9), 1.0e9));
   p.f0 = static_cast<float>(ux - fx);
   p.g0 = static_cast<float>(uy - fy);
-  if (!(ux == ux) || !(uy == uy)) { p.i0 = -2000000000; p.f0 = 0.0f; }
+  if (!(ux == ux) || !(uy == uy)) { p.fi0 = -2.0e9f; p.f0 = 0.0f; }
   return p;
 }
 
 // Cell index and in-cell fractions at offset (px, py) from the origin; false
-// when outside the grid's cells.
+// when outside the grid's cells.  The cell's coordinates are integral floats
+// (exact sums), tested against the grid's bounds and converted once.
 __device__ __forceinline__ bool locate(const PackedGrid &g, const GridPos &p, float px, float py,
                                        int64_t *cell, float *fx, float *fy) {
   const float ux = fmaf(px, g.inv_sp_x, p.f0);
   const float uy = fmaf(py, g.inv_sp_y, p.g0);
   const float flx = floorf(ux), fly = floorf(uy);
-  const float cx = static_cast<float>(p.i0) + flx, cy = static_cast<float>(p.j0) + fly;
-  if (!(cx >= 0.0f && cx <= static_cast<float>(g.nx - 2) && cy >= 0.0f &&
-        cy <= static_cast<float>(g.ny - 2)))
-    return false;
-  *cell = static_cast<int64_t>(p.j0 + static_cast<int>(fly)) * (g.nx - 1) +
-          (p.i0 + static_cast<int>(flx));
+  const float cx = p.fi0 + flx, cy = p.fj0 + fly;
+  if (!(cx >= 0.0f && cx <= g.cx_max && cy >= 0.0f && cy <= g.cy_max)) return false;
+  *cell = static_cast<int64_t>(static_cast<int>(cy)) * (g.nx - 1) + static_cast<int>(cx);
   *fx = ux - flx;
   *fy = uy - fly;
   return true;
@@ -274,11 +273,19 @@ __device__ __forceinline__ int32_t save_period(const BatchArgs &a) {
   return a.decimation > 0x7fffffff ? 0x7fffffff : static_cast<int32_t>(a.decimation);
 }
 
+// A lane's scenario: from the kernel's parameters in the single-scenario
+// build (ONE), else from the device table.
+template <bool ONE>
+__device__ __forceinline__ const ScenarioDev &scenario(const BatchArgs &a, int s) {
+  return ONE ? a.scen0 : a.scen[s];
+}
+
+template <bool ONE>
 __device__ __forceinline__ void start(const BatchArgs &a, RayLane &L, int64_t r) {
   L.ray = r;
-  L.scen = a.ray_scenario ? static_cast<int>(a.ray_scenario[r]) : 0;
+  L.scen = (!ONE && a.ray_scenario) ? static_cast<int>(a.ray_scenario[r]) : 0;
   if (L.scen >= a.n_scenarios) L.scen = 0;
-  const ScenarioDev &s = a.scen[L.scen];
+  const ScenarioDev &s = scenario<ONE>(a, L.scen);
   L.ox = a.x0[r];
   L.oy = a.y0[r];
   L.px = L.py = L.cpx = L.cpy = L.ckx = L.cky = 0.0f;
@@ -298,8 +305,9 @@ __device__ __forceinline__ void start(const BatchArgs &a, RayLane &L, int64_t r)
 }
 
 // One RK4 step of lane L.  Returns BATCH_COMPLETE while the ray goes on.
+template <bool ONE>
 __device__ __forceinline__ int advance(const BatchArgs &a, RayLane &L) {
-  const ScenarioDev &s = a.scen[L.scen];
+  const ScenarioDev &s = scenario<ONE>(a, L.scen);
   // step constants in FP32 from the host (a conversion here would run on the
   // FP64 pipe, and the compiler re-derives such values under register pressure)
   const float dt = a.dt_f;
@@ -336,7 +344,7 @@ __device__ __forceinline__ int advance(const BatchArgs &a, RayLane &L) {
   return BATCH_COMPLETE;
 }
 
-template <int RPT>
+template <int RPT, bool ONE>
 __device__ __forceinline__ void k2_body(const BatchArgs &a) {
   const int lane = threadIdx.x & 31;
   const unsigned lt_mask = (1u << lane) - 1u;
@@ -356,7 +364,7 @@ __device__ __forceinline__ void k2_body(const BatchArgs &a) {
         base = __shfl_sync(kFull, base, leader);
         if (L[j].ray == -1) {
           const int64_t r = static_cast<int64_t>(base) + __popc(need & lt_mask);
-          if (r < n) start(a, L[j], a.order ? static_cast<int64_t>(__ldg(a.order + r)) : r);
+          if (r < n) start<ONE>(a, L[j], a.order ? static_cast<int64_t>(__ldg(a.order + r)) : r);
           else L[j].ray = -2;
         }
       }
@@ -372,7 +380,7 @@ __device__ __forceinline__ void k2_body(const BatchArgs &a) {
         finish(a, L[j], BATCH_COMPLETE);
         continue;
       }
-      const int st = advance(a, L[j]);
+      const int st = advance<ONE>(a, L[j]);
       if (st != BATCH_COMPLETE) finish(a, L[j], st);
     }
   }
@@ -389,10 +397,15 @@ __device__ __forceinline__ void k2_body(const BatchArgs &a) {
 // lanes the spills only add latency (65,536-ray seamount: 22.2 -> 19.3).
 // The launcher takes the capped build when the launch asks for more blocks
 // per SM than the uncapped one holds.
-__global__ void __launch_bounds__(256) rk4_f32_kernel_1(BatchArgs a) { k2_body<1>(a); }
-__global__ void __maxnreg__(72) rk4_f32_kernel_1r(BatchArgs a) { k2_body<1>(a); }
+// Each has a single-scenario form (ONE: the scenario's fields are operands
+// from the kernel's parameters instead of loads at every lookup).
+template <bool ONE>
+__global__ void __launch_bounds__(256) rk4_f32_kernel_1(BatchArgs a) { k2_body<1, ONE>(a); }
+template <bool ONE>
+__global__ void __maxnreg__(72) rk4_f32_kernel_1r(BatchArgs a) { k2_body<1, ONE>(a); }
 // Two rays per lane hold twice the lane state: no cap.
-__global__ void __launch_bounds__(256) rk4_f32_kernel_2(BatchArgs a) { k2_body<2>(a); }
+template <bool ONE>
+__global__ void __launch_bounds__(256) rk4_f32_kernel_2(BatchArgs a) { k2_body<2, ONE>(a); }
 
 }  // namespace
 
@@ -437,13 +450,14 @@ cudaError_t launch_fill_nan(float *p, int64_t count, cudaStream_t stream) {
 // up to 256), queried once; 0: not yet known.
 static std::atomic<int> g_resident_1[9];
 
-const void *rk4_f32_function(int rays_per_lane, int block, int blocks_per_sm) {
-  if (rays_per_lane == 2) return reinterpret_cast<const void *>(&rk4_f32_kernel_2);
+template <bool ONE>
+static const void *k2_function(int rays_per_lane, int block, int blocks_per_sm) {
+  if (rays_per_lane == 2) return reinterpret_cast<const void *>(&rk4_f32_kernel_2<ONE>);
   const int slot = (block >= 32 && block <= 256 && block % 32 == 0) ? block / 32 : 0;
   int resident = slot ? g_resident_1[slot].load(std::memory_order_relaxed) : 0;
   if (resident == 0) {
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, rk4_f32_kernel_1, block, 0) !=
-            cudaSuccess ||
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, rk4_f32_kernel_1<false>, block,
+                                                      0) != cudaSuccess ||
         resident < 1) {
       (void)cudaGetLastError();
       resident = blocks_per_sm;  // unknown: the uncapped build
@@ -451,8 +465,14 @@ const void *rk4_f32_function(int rays_per_lane, int block, int blocks_per_sm) {
       g_resident_1[slot].store(resident, std::memory_order_relaxed);
     }
   }
-  return resident < blocks_per_sm ? reinterpret_cast<const void *>(&rk4_f32_kernel_1r)
-                                  : reinterpret_cast<const void *>(&rk4_f32_kernel_1);
+  return resident < blocks_per_sm ? reinterpret_cast<const void *>(&rk4_f32_kernel_1r<ONE>)
+                                  : reinterpret_cast<const void *>(&rk4_f32_kernel_1<ONE>);
+}
+
+const void *rk4_f32_function(int rays_per_lane, int block, int blocks_per_sm,
+                             int n_scenarios) {
+  return n_scenarios == 1 ? k2_function<true>(rays_per_lane, block, blocks_per_sm)
+                          : k2_function<false>(rays_per_lane, block, blocks_per_sm);
 }
 
 cudaError_t launch_rk4_f32(const BatchArgs &a, int block, int blocks_per_sm, int rays_per_lane,
@@ -464,8 +484,8 @@ cudaError_t launch_rk4_f32(const BatchArgs &a, int block, int blocks_per_sm, int
   if (e != cudaSuccess) return e;
   const unsigned grid = static_cast<unsigned>(sms * blocks_per_sm);
   void *args[] = {const_cast<BatchArgs *>(&a)};
-  return cudaLaunchKernel(rk4_f32_function(rays_per_lane, block, blocks_per_sm), dim3(grid),
-                          dim3(block), args, 0, stream);
+  return cudaLaunchKernel(rk4_f32_function(rays_per_lane, block, blocks_per_sm, a.n_scenarios),
+                          dim3(grid), dim3(block), args, 0, stream);
 }
 
 }  // namespace mr

@@ -261,6 +261,31 @@ def test_constant_depth_circle(mr, oracle, depth):
     check_circle(r[0], r[1], rays[2], rays[3])
 
 
+@pytest.mark.parametrize("t0,t_end,dt", [
+    (0.0, 0.0, 1.0),      # zero duration: the initial row only
+    (0.0, 10.25, 1.0),    # fractional: ceil(10.25 / 1) = 11 steps, the last past t_end
+    (0.0, 0.5, 2.0),      # one step longer than the whole duration
+    (37.5, 87.5, 0.5),    # a start time other than 0 (t accumulates from t0)
+])
+def test_durations_and_start_times(mr, oracle, t0, t_end, dt):
+    # the stepper's step count and time rows (ceil((t_end - t0) / dt) steps,
+    # t += dt) on a grid with a current, rays of several directions
+    from mantaray_gb300.workloads import seamount
+
+    w = seamount(n_rays=64, steps=10)
+    bathy = ("grid", w.bx, w.by, w.depth)
+    current = ("grid", w.cx, w.cy, w.u, w.v)
+    r = both(mr, oracle, bathy, current, w.x0 + 500.0, w.y0, w.kx0, w.ky0, t0, t_end, dt)
+    check(*r)
+    steps = math.ceil((t_end - t0) / dt)
+    assert r[0].shape[1] == steps + 1
+    assert np.all(r[1] == steps + 1)
+    t = t0
+    for row in range(steps + 1):
+        assert np.all(r[0][0, row] == t)
+        t = t + dt
+
+
 def test_slope_and_many_waves(mr, oracle):
     # src/ray.rs:550-584 and :1331-1361
     r = both(mr, oracle, ("slope",), ZERO, 10.0, 1000.0, 0.1, 0.0, 0.0, 100.0, 1.0)
