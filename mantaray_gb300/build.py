@@ -26,13 +26,16 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", INCLUDE
 # Translation units and their extra flags.  The integrators are compiled with
 # -fmad=false: the plain kernel because the reference (Rust) never contracts
 # a*b+c, the batched kernel so that its explicit fmaf calls are its only
-# fused operations (same bits for every launch shape).
+# fused operations (same bits for every launch shape).  Its single-scenario
+# builds (rk4_f32_one.cu) also flush FP32 subnormals (-ftz=true; the file
+# says why).
 UNITS = {
     "rk4_f64.cu": ["-fmad=false"],
     "api.cu": [],
     "netcdf3.cpp": [],
     "diag.cu": [],
     "rk4_f32.cu": ["-fmad=false"],
+    "rk4_f32_one.cu": ["-fmad=false", "-ftz=true"],
     "batch_api.cu": [],
     "batch_static.cu": [],
     "diff.cu": [],

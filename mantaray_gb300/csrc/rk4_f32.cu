@@ -3,10 +3,12 @@
 // K5 (pack_*_cells): repacks a bathymetry / current grid of the plain form
 // (f64 values in HBM) into the cell records of batch.h, one thread per cell.
 //
-// K2 (rk4_f32_kernel_1 / _1r / _2): a persistent kernel, grid = SMs x
-// blocks per SM.  Each lane holds 1 or 2 rays (_2); one ray per lane has an
-// uncapped and a 72-register build (_1r), chosen by the launch shape.  A lane whose ray has ended refills from
-// a device work queue: the warp ballots its empty slots, one lane reserves
+// K2 (rk4_f32_kernel_1 / _1r / _2, device code in k2.cuh): a persistent
+// kernel, grid = SMs x blocks per SM.  Each lane holds 1 or 2 rays (_2); one
+// ray per lane has an uncapped and a 72-register build (_1r), chosen by the
+// launch shape.  Each build has a scenario-table form (instantiated here) and
+// a single-scenario form (rk4_f32_one.cu).  A lane whose ray has ended
+// refills from a device work queue: the warp ballots its empty slots, one lane reserves
 // that many ray indices with a single atomicAdd and the indices are handed out
 // by rank within the ballot, so lanes never idle while work remains and rays
 // of very different lifetimes (domain exits, dry cells) keep every lane busy.
@@ -95,319 +97,13 @@ __global__ void pack_current_cells(CurrentDev cu, float4 *cells) {
   cells[3 * c + 2] = r2;
 }
 
-// ------------------------------------------------------------------ K2 --
-
-constexpr unsigned kFull = 0xffffffffu;
-constexpr float kGf = 9.8f;
-
-// Position of a lane on one grid: the cell of its origin (integral floats:
-// exact, grids have fewer than 2^24 points per axis) plus the origin's
-// fractional cell offset.
-struct GridPos {
-  float fi0, fj0;
-  float f0, g0;
-};
-
-__device__ __forceinline__ GridPos grid_pos(const PackedGrid &g, double ox, double oy) {
-  GridPos p;
-  const double ux = (ox - g.x0) * g.inv_sp_xd, uy = (oy - g.y0) * g.inv_sp_yd;
-  const double fx = floor(ux), fy = floor(uy);
-  // clamp far-away origins (+-1e9 is exact in FP32); such a lane fails the
-  // in-range test of its first lookup
-  p.fi0 = static_cast<float>(fmin(fmax(fx, -1.0e9), 1.0e9));
-  p.fj0 = static_cast<float>(fmin(fmax(fy, -1.0e9), 1.0e9));
-  p.f0 = static_cast<float>(ux - fx);
-  p.g0 = static_cast<float>(uy - fy);
-  if (!(ux == ux) || !(uy == uy)) { p.fi0 = -2.0e9f; p.f0 = 0.0f; }
-  return p;
-}
-
-// Cell index and in-cell fractions at offset (px, py) from the origin; false
-// when outside the grid's cells.  The cell's coordinates are integral floats
-// (exact sums), tested against the grid's bounds and converted once.
-__device__ __forceinline__ bool locate(const PackedGrid &g, const GridPos &p, float px, float py,
-                                       int64_t *cell, float *fx, float *fy) {
-  const float ux = fmaf(px, g.inv_sp_x, p.f0);
-  const float uy = fmaf(py, g.inv_sp_y, p.g0);
-  const float flx = floorf(ux), fly = floorf(uy);
-  const float cx = p.fi0 + flx, cy = p.fj0 + fly;
-  if (!(cx >= 0.0f && cx <= g.cx_max && cy >= 0.0f && cy <= g.cy_max)) return false;
-  *cell = static_cast<int64_t>(static_cast<int>(cy)) * (g.nx - 1) + static_cast<int>(cx);
-  *fx = ux - flx;
-  *fy = uy - fly;
-  return true;
-}
-
-__device__ __forceinline__ float bilin(const float4 &v, float fx, float fy) {
-  // v = (v(i,j), v(i+1,j), v(i,j+1), v(i+1,j+1))
-  const float a = fmaf(fx, v.y - v.x, v.x);
-  const float b = fmaf(fx, v.w - v.z, v.z);
-  return fmaf(fy, b - a, a);
-}
-
-// The cell records a lane read last, kept in registers: a ray stays in one
-// cell for several steps, so most stage lookups reuse them instead of
-// loading them again (same values, no memory latency on the dependent chain).
-struct CellCache {
-  int64_t bkey, ckey;     // cell indices held, -1: none
-  float4 b0;              // depth corners
-  float bx, by;           // dh/dx, dh/dy
-  float4 c0, c1, c2;      // u corners, v corners, gradients
-};
-
-struct RayLane {
-  int64_t ray;      // -1: empty slot, -2: no work left
-  int scen;
-  double ox, oy;    // FP64 origin
-  GridPos pb, pc;   // origin on the bathymetry and current grids
-  float px, py, kx, ky;      // offsets and wavenumber
-  float cpx, cpy, ckx, cky;  // Kahan compensations
-  int64_t step;
-  int32_t saved;
-  int32_t to_save;    // steps until the next decimated row (no 64-bit modulo per step)
-  int32_t to_rebase;  // steps until the next origin rebase
-  CellCache cache;
-};
-
-// Right-hand side in FP32 at offset (px, py); returns a BatchStatus.
-__device__ __forceinline__ int rhs_f32(const ScenarioDev &s, RayLane &L, float px, float py,
-                                       float kx, float ky, float d[4]) {
-  int64_t cb;
-  float fx, fy;
-  if (!locate(s.bathy, L.pb, px, py, &cb, &fx, &fy)) return BATCH_OUT_OF_DOMAIN;
-  CellCache &C = L.cache;
-  if (cb != C.bkey) {
-    C.b0 = __ldg(s.bathy.cells + 2 * cb);
-    const float4 b1 = __ldg(s.bathy.cells + 2 * cb + 1);
-    C.bx = b1.x;
-    C.by = b1.y;
-    C.bkey = cb;
-  }
-  const float h = bilin(C.b0, fx, fy);
-  float u, v, dudx = 0.0f, dudy = 0.0f, dvdx = 0.0f, dvdy = 0.0f;
-  if (s.current.kind == 0) {
-    int64_t cc = cb;
-    float gx = fx, gy = fy;  // the same cell when the grids coincide (same origin, same arithmetic)
-    if (!s.same_grid && !locate(s.current, L.pc, px, py, &cc, &gx, &gy))
-      return BATCH_OUT_OF_DOMAIN;
-    if (cc != C.ckey) {
-      C.c0 = __ldg(s.current.cells + 3 * cc);
-      C.c1 = __ldg(s.current.cells + 3 * cc + 1);
-      C.c2 = __ldg(s.current.cells + 3 * cc + 2);
-      C.ckey = cc;
-    }
-    u = bilin(C.c0, gx, gy);
-    v = bilin(C.c1, gx, gy);
-    dudx = C.c2.x; dudy = C.c2.y; dvdx = C.c2.z; dvdy = C.c2.w;
-  } else {
-    u = s.current.cu;
-    v = s.current.cv;
-  }
-  if (!(h > 0.0f)) return h <= 0.0f ? BATCH_DRY : BATCH_OUT_OF_DOMAIN;
-  const float k2 = fmaf(kx, kx, ky * ky);
-  if (!(k2 > 0.0f) || !(k2 < 3.0e38f)) return BATCH_BAD_WAVENUMBER;
-  const float rk = rsqrtf(k2);
-  const float k = k2 * rk;
-  const float kh = k * h;
-  const float m = -expm1f(-2.0f * kh);  // 1 - exp(-2kh)
-  const float q = 1.0f - m;
-  const float inv_d = __frcp_rn(m * (2.0f - m));  // = 1.0f / x, correctly rounded
-  const float r = m * inv_d;            // 1 / (2 - m)
-  const float th = m * r;               // tanh(kh)
-  const float gkt = kGf * k * th;
-  const float rs = rsqrtf(gkt);
-  const float q4 = 4.0f * q;
-  // kh / cosh^2(kh) = 4 kh q r^2 and 1 / (sinh(kh) cosh(kh)) = 4 q inv_d
-  const float cg = (0.5f * kGf) * (fmaf(kh * q4, r * r, th) * rs);
-  const float f = (-0.5f * k) * ((q4 * inv_d) * (gkt * rs));
-  const float cgk = cg * rk;            // c_g / k: c_g cos(theta) = cgk kx
-  d[0] = fmaf(cgk, kx, u);
-  d[1] = fmaf(cgk, ky, v);
-  d[2] = fmaf(-ky, dvdx, fmaf(-kx, dudx, f * C.bx));
-  d[3] = fmaf(-ky, dvdy, fmaf(-kx, dudy, f * C.by));
-  return BATCH_COMPLETE;
-}
-
-__device__ __forceinline__ void kahan_add(float &sum, float &comp, float inc) {
-  const float y = inc - comp;
-  const float t = sum + y;
-  comp = (t - sum) - y;
-  sum = t;
-}
-
-__device__ __forceinline__ void rebase(const ScenarioDev &s, RayLane &L) {
-  L.ox += static_cast<double>(L.px) - static_cast<double>(L.cpx);
-  L.oy += static_cast<double>(L.py) - static_cast<double>(L.cpy);
-  L.px = L.py = L.cpx = L.cpy = 0.0f;
-  L.pb = grid_pos(s.bathy, L.ox, L.oy);
-  L.pc = s.same_grid ? L.pb : grid_pos(s.current, L.ox, L.oy);
-}
-
-__device__ __forceinline__ void save_row(const BatchArgs &a, const RayLane &L) {
-  if (L.saved >= a.save_cap) return;
-  const int64_t plane = a.save_cap * a.n_stride;
-  float *p = a.saved + static_cast<int64_t>(L.saved) * a.n_stride + L.ray;
-  p[0] = static_cast<float>(a.t0 + static_cast<double>(L.step) * a.dt);
-  p[plane] = static_cast<float>(L.ox + (static_cast<double>(L.px) - static_cast<double>(L.cpx)));
-  p[2 * plane] = static_cast<float>(L.oy + (static_cast<double>(L.py) - static_cast<double>(L.cpy)));
-  p[3 * plane] = L.kx - L.ckx;
-  p[4 * plane] = L.ky - L.cky;
-}
-
-__device__ __forceinline__ void finish(const BatchArgs &a, RayLane &L, int status) {
-  const int64_t r = L.ray;
-  a.end_state[r] = a.t0 + static_cast<double>(L.step) * a.dt;
-  a.end_state[a.n_stride + r] = L.ox + (static_cast<double>(L.px) - static_cast<double>(L.cpx));
-  a.end_state[2 * a.n_stride + r] = L.oy + (static_cast<double>(L.py) - static_cast<double>(L.cpy));
-  a.end_state[3 * a.n_stride + r] = static_cast<double>(L.kx) - static_cast<double>(L.ckx);
-  a.end_state[4 * a.n_stride + r] = static_cast<double>(L.ky) - static_cast<double>(L.cky);
-  a.n_steps[r] = static_cast<int32_t>(L.step);
-  a.n_saved[r] = L.saved;
-  a.status[r] = static_cast<uint8_t>(status);
-  L.ray = -1;
-}
-
-// The decimation as a step countdown (a ray takes fewer than 2^31 steps, so
-// a larger decimation saves no row after step 0 either way).
-__device__ __forceinline__ int32_t save_period(const BatchArgs &a) {
-  return a.decimation > 0x7fffffff ? 0x7fffffff : static_cast<int32_t>(a.decimation);
-}
-
-// A lane's scenario: from the kernel's parameters in the single-scenario
-// build (ONE), else from the device table.
-template <bool ONE>
-__device__ __forceinline__ const ScenarioDev &scenario(const BatchArgs &a, int s) {
-  return ONE ? a.scen0 : a.scen[s];
-}
-
-template <bool ONE>
-__device__ __forceinline__ void start(const BatchArgs &a, RayLane &L, int64_t r) {
-  L.ray = r;
-  L.scen = (!ONE && a.ray_scenario) ? static_cast<int>(a.ray_scenario[r]) : 0;
-  if (L.scen >= a.n_scenarios) L.scen = 0;
-  const ScenarioDev &s = scenario<ONE>(a, L.scen);
-  L.ox = a.x0[r];
-  L.oy = a.y0[r];
-  L.px = L.py = L.cpx = L.cpy = L.ckx = L.cky = 0.0f;
-  L.kx = static_cast<float>(a.kx0[r]);
-  L.ky = static_cast<float>(a.ky0[r]);
-  L.pb = grid_pos(s.bathy, L.ox, L.oy);
-  L.pc = s.same_grid ? L.pb : grid_pos(s.current, L.ox, L.oy);
-  L.step = 0;
-  L.saved = 0;
-  L.cache.bkey = L.cache.ckey = -1;
-  L.to_save = save_period(a);
-  L.to_rebase = a.rebase_interval;
-  if (a.decimation > 0) {
-    save_row(a, L);
-    L.saved = 1;
-  }
-}
-
-// One RK4 step of lane L.  Returns BATCH_COMPLETE while the ray goes on.
-template <bool ONE>
-__device__ __forceinline__ int advance(const BatchArgs &a, RayLane &L) {
-  const ScenarioDev &s = scenario<ONE>(a, L.scen);
-  // step constants in FP32 from the host (a conversion here would run on the
-  // FP64 pipe, and the compiler re-derives such values under register pressure)
-  const float dt = a.dt_f;
-  const float half = a.half_f;
-  float k1[4], k2[4], k3[4], k4[4];
-  int st = rhs_f32(s, L, L.px, L.py, L.kx, L.ky, k1);
-  if (st == BATCH_COMPLETE)
-    st = rhs_f32(s, L, fmaf(half, k1[0], L.px), fmaf(half, k1[1], L.py),
-                 fmaf(half, k1[2], L.kx), fmaf(half, k1[3], L.ky), k2);
-  if (st == BATCH_COMPLETE)
-    st = rhs_f32(s, L, fmaf(half, k2[0], L.px), fmaf(half, k2[1], L.py),
-                 fmaf(half, k2[2], L.kx), fmaf(half, k2[3], L.ky), k3);
-  if (st == BATCH_COMPLETE)
-    st = rhs_f32(s, L, fmaf(dt, k3[0], L.px), fmaf(dt, k3[1], L.py), fmaf(dt, k3[2], L.kx),
-                 fmaf(dt, k3[3], L.ky), k4);
-  if (st != BATCH_COMPLETE) return st;
-  const float sixth = a.sixth_f;
-#pragma unroll
-  for (int q = 0; q < 4; ++q) k1[q] = sixth * fmaf(2.0f, k2[q] + k3[q], k1[q] + k4[q]);
-  kahan_add(L.px, L.cpx, k1[0]);
-  kahan_add(L.py, L.cpy, k1[1]);
-  kahan_add(L.kx, L.ckx, k1[2]);
-  kahan_add(L.ky, L.cky, k1[3]);
-  ++L.step;
-  if (a.decimation > 0 && --L.to_save == 0) {
-    L.to_save = save_period(a);
-    save_row(a, L);
-    ++L.saved;
-  }
-  if (--L.to_rebase == 0) {
-    L.to_rebase = a.rebase_interval;
-    rebase(s, L);
-  }
-  return BATCH_COMPLETE;
-}
-
-template <int RPT, bool ONE>
-__device__ __forceinline__ void k2_body(const BatchArgs &a) {
-  const int lane = threadIdx.x & 31;
-  const unsigned lt_mask = (1u << lane) - 1u;
-  const int64_t n = a.n;
-  RayLane L[RPT];
-#pragma unroll
-  for (int j = 0; j < RPT; ++j) L[j].ray = -1;
-  while (true) {
-    // refill empty slots from the work queue, one atomic per warp and slot
-#pragma unroll
-    for (int j = 0; j < RPT; ++j) {
-      const unsigned need = __ballot_sync(kFull, L[j].ray == -1);
-      if (need) {
-        const int leader = __ffs(need) - 1;
-        unsigned long long base = 0;
-        if (lane == leader) base = atomicAdd(a.queue, static_cast<unsigned long long>(__popc(need)));
-        base = __shfl_sync(kFull, base, leader);
-        if (L[j].ray == -1) {
-          const int64_t r = static_cast<int64_t>(base) + __popc(need & lt_mask);
-          if (r < n) start<ONE>(a, L[j], a.order ? static_cast<int64_t>(__ldg(a.order + r)) : r);
-          else L[j].ray = -2;
-        }
-      }
-    }
-    bool live = false;
-#pragma unroll
-    for (int j = 0; j < RPT; ++j) live |= L[j].ray >= 0;
-    if (!__any_sync(kFull, live)) break;
-#pragma unroll
-    for (int j = 0; j < RPT; ++j) {
-      if (L[j].ray < 0) continue;
-      if (L[j].step >= a.max_steps) {
-        finish(a, L[j], BATCH_COMPLETE);
-        continue;
-      }
-      const int st = advance<ONE>(a, L[j]);
-      if (st != BATCH_COMPLETE) finish(a, L[j], st);
-    }
-  }
-}
-
-// One ray per lane, two builds.  rk4_f32_kernel_1 takes the compiler's
-// register count (~100: 4 blocks of 128 threads, 16 warps, per SM).
-// rk4_f32_kernel_1r is capped at 72 registers (28 warps per SM; 80 B
-// spilled to L1).  The kernel is issue- and latency-bound; when a call has
-// rays for more warps than the first keeps resident, the extra warps hide
-// more of the dependent FP32 chains than the spills cost (4,096^2
-// shelf-slope, 2^20 rays: 30.6 -> 32.7 G ray-steps/s at 128 x 8; caps of
-// 80 / 64 / 56 registers gave 32.0 / 32.7 / 31.5); with fewer rays than
-// lanes the spills only add latency (65,536-ray seamount: 22.2 -> 19.3).
-// The launcher takes the capped build when the launch asks for more blocks
-// per SM than the uncapped one holds.
-// Each has a single-scenario form (ONE: the scenario's fields are operands
-// from the kernel's parameters instead of loads at every lookup).
-template <bool ONE>
-__global__ void __launch_bounds__(256) rk4_f32_kernel_1(BatchArgs a) { k2_body<1, ONE>(a); }
-template <bool ONE>
-__global__ void __maxnreg__(72) rk4_f32_kernel_1r(BatchArgs a) { k2_body<1, ONE>(a); }
-// Two rays per lane hold twice the lane state: no cap.
-template <bool ONE>
-__global__ void __launch_bounds__(256) rk4_f32_kernel_2(BatchArgs a) { k2_body<2, ONE>(a); }
-
 }  // namespace
+
+}  // namespace mr
+
+#include "k2.cuh"
+
+namespace mr {
 
 cudaError_t launch_pack_bathy(const BathyDev &b, float4 *cells, cudaStream_t stream) {
   const int64_t ncell = static_cast<int64_t>(b.nx - 1) * static_cast<int64_t>(b.ny - 1);
@@ -446,33 +142,36 @@ cudaError_t launch_fill_nan(float *p, int64_t count, cudaStream_t stream) {
   return cudaGetLastError();
 }
 
-// Resident blocks per SM of rk4_f32_kernel_1 by block size (multiples of 32
-// up to 256), queried once; 0: not yet known.
-static std::atomic<int> g_resident_1[9];
+// The three builds of one form: [0] one ray per lane, uncapped; [1] the
+// same capped at 72 registers; [2] two rays per lane.
+static const void *table_builds[3] = {
+    reinterpret_cast<const void *>(&rk4_f32_kernel_1<false>),
+    reinterpret_cast<const void *>(&rk4_f32_kernel_1r<false>),
+    reinterpret_cast<const void *>(&rk4_f32_kernel_2<false>)};
 
-template <bool ONE>
-static const void *k2_function(int rays_per_lane, int block, int blocks_per_sm) {
-  if (rays_per_lane == 2) return reinterpret_cast<const void *>(&rk4_f32_kernel_2<ONE>);
+// Resident blocks per SM of each form's uncapped one-ray build by block
+// size (multiples of 32 up to 256), queried once; 0: not yet known.
+static std::atomic<int> g_resident_1[2][9];
+
+const void *rk4_f32_function(int rays_per_lane, int block, int blocks_per_sm,
+                             int n_scenarios) {
+  const int one = n_scenarios == 1 ? 1 : 0;
+  const void *fn[3];
+  for (int k = 0; k < 3; ++k) fn[k] = one ? rk4_f32_one_function(k) : table_builds[k];
+  if (rays_per_lane == 2) return fn[2];
   const int slot = (block >= 32 && block <= 256 && block % 32 == 0) ? block / 32 : 0;
-  int resident = slot ? g_resident_1[slot].load(std::memory_order_relaxed) : 0;
+  int resident = slot ? g_resident_1[one][slot].load(std::memory_order_relaxed) : 0;
   if (resident == 0) {
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, rk4_f32_kernel_1<false>, block,
-                                                      0) != cudaSuccess ||
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, fn[0], block, 0) !=
+            cudaSuccess ||
         resident < 1) {
       (void)cudaGetLastError();
       resident = blocks_per_sm;  // unknown: the uncapped build
     } else if (slot) {
-      g_resident_1[slot].store(resident, std::memory_order_relaxed);
+      g_resident_1[one][slot].store(resident, std::memory_order_relaxed);
     }
   }
-  return resident < blocks_per_sm ? reinterpret_cast<const void *>(&rk4_f32_kernel_1r<ONE>)
-                                  : reinterpret_cast<const void *>(&rk4_f32_kernel_1<ONE>);
-}
-
-const void *rk4_f32_function(int rays_per_lane, int block, int blocks_per_sm,
-                             int n_scenarios) {
-  return n_scenarios == 1 ? k2_function<true>(rays_per_lane, block, blocks_per_sm)
-                          : k2_function<false>(rays_per_lane, block, blocks_per_sm);
+  return resident < blocks_per_sm ? fn[1] : fn[0];
 }
 
 cudaError_t launch_rk4_f32(const BatchArgs &a, int block, int blocks_per_sm, int rays_per_lane,
