@@ -44,7 +44,7 @@ OUT_BYTES_PER_ROW = 5 * 8
 # FP32 floating-point operations one ray-step of the batched kernel executes
 # (FADD/FMUL = 1, FFMA = 2), counted by ncu on the 4,096^2 shelf-slope case
 # with the current on the bathymetry's grid.
-FP32_FLOP_PER_RAY_STEP = 484.0
+FP32_FLOP_PER_RAY_STEP = 468.2
 # Algorithmic work of one ray-step (the reference's arithmetic, hand count from
 # src/wave_ray_path.rs:118-216 plus the RK4 update): ~55 FP64 add/mul/div per
 # right-hand side x 4 + ~53 for the update = 270 (36 transcendental calls not
@@ -57,9 +57,9 @@ ALG_FP32_FLOP_PER_RAY_STEP = 710.0
 # DFMA = 2), per right-hand-side arithmetic, counted by ncu on the plain
 # kernel over the seamount workload (65,536 rays x 100 steps)
 # (sm__sass_thread_inst_executed_op_d{add,mul,fma}_pred_on; profiles/).
-FP64_FLOP_PER_RAY_STEP = {"libm": 1818.1, "identity": 343.6}
+FP64_FLOP_PER_RAY_STEP = {"libm": 1401.4, "identity": 343.6}
 # FP64-pipe instructions per ray-step (sm__inst_executed_pipe_fp64 x 32, same captures)
-FP64_PIPE_INST_PER_RAY_STEP = {"libm": 1217.9, "identity": 283.6}
+FP64_PIPE_INST_PER_RAY_STEP = {"libm": 945.2, "identity": 283.6}
 
 
 def parse():
@@ -700,7 +700,7 @@ def batched_arm(args, rank: int, world: int, local_rank: int):
     # DRAM bytes per ray-step of ncu captures (profiles/), scaled to one call's ray-steps
     k2_dram_per_ray_step = {"seamount": (18.60e6 / (65536 * 400),
                                          "65,536-ray x 400-step seamount capture"),
-                            "shelf_slope": ((506.21e6 + 43.11e6) / 330.35e6,
+                            "shelf_slope": ((460.32e6 + 44.54e6) / 330.35e6,
                                             "4,096^2-grid, 2^20-ray x 400-step shelf-slope "
                                             "capture")}
     if args.workload in k2_dram_per_ray_step:

@@ -4,7 +4,9 @@
 // bit-exact field lookups (lookup.cuh):
 //  - RhsLibm: the reference's expression, operation for operation, with its
 //    calls to sqrt, atan2, cos, sin, cosh, tanh and sinh (CUDA's versions,
-//    within an ulp or two of glibc's);
+//    within an ulp or two of glibc's; cos and sin of the one angle from
+//    sincos, and each call the reference repeats on the same argument made
+//    once);
 //  - RhsIdentity: the same quantities through exact identities that need
 //    fewer FP64 instructions -- cos(atan2(ky, kx)) = kx/k,
 //    sin(atan2(ky, kx)) = ky/k, and with a = kh, q = exp(-2a) from the single
@@ -52,20 +54,26 @@ struct RhsLibm {
     if (e) return e;
     const double k = sqrt(kx * kx + ky * ky);
     const double theta = atan2(ky, kx);
+    // kh, cosh(kh), tanh(kh) and sqrt(g k tanh(kh)) appear in both
+    // group_velocity and dkdt_bathy: each is evaluated once (the same
+    // function of the same argument gives the same value, and k * kG equals
+    // kG * k exactly, so sqrt(k * kG * th) is sqrt(kG * k * tanh(kh)))
+    const double kh = k * h;
+    const double ch = cosh(kh);
+    const double th = tanh(kh);
+    const double sq = sqrt(kG * k * th);
     double cg;
     if (h <= 0.0) {
       cg = f64_nan();
     } else {
       if (k <= 0.0) return RHS_ARGUMENT_OUT_OF_BOUNDS;
-      const double kh = k * h;
-      const double ch = cosh(kh);
-      const double th = tanh(kh);
-      cg = (kG / 2.0) * ((th + kh / (ch * ch)) / sqrt(k * kG * th));
+      cg = (kG / 2.0) * ((th + kh / (ch * ch)) / sq);
     }
-    const double cgx = cg * cos(theta) + cur[0];
-    const double cgy = cg * sin(theta) + cur[1];
-    const double kh = k * h;
-    const double f = (-0.5) * k * 1.0 / sinh(kh) * 1.0 / cosh(kh) * sqrt(kG * k * tanh(kh));
+    double st, ct;
+    sincos(theta, &st, &ct);
+    const double cgx = cg * ct + cur[0];
+    const double cgy = cg * st + cur[1];
+    const double f = (-0.5) * k * 1.0 / sinh(kh) * 1.0 / ch * sq;
     out[0] = cgx;
     out[1] = cgy;
     out[2] = f * dhdx - kx * cur[2] - ky * cur[4];
