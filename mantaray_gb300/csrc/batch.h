@@ -5,10 +5,14 @@
 // indexed by its south-west corner (i, j), holding everything a lookup
 // inside that square needs, so a lookup is a few 16-byte loads from one
 // contiguous record:
-//   bathymetry cell (8 floats, 32 B):  h(i,j) h(i+1,j) h(i,j+1) h(i+1,j+1)
+//   bathymetry cell (8 floats, 32 B):  h's bilinear coefficients c0 c1 c2 c3
 //                                      dh/dx dh/dy 0 0
-//   current cell (12 floats, 48 B):    u x4, v x4 (same corner order),
+//   current cell (12 floats, 48 B):    u's coefficients x4, v's x4,
 //                                      du/dx du/dy dv/dx dv/dy
+// where a field inside the cell is c0 + c1 fx + c2 fy + c3 fx fy at the
+// cell fractions (fx, fy): c0 = v(i,j), c1 = v(i+1,j) - v(i,j),
+// c2 = v(i,j+1) - v(i,j), c3 = v(i+1,j+1) - v(i+1,j) - v(i,j+1) + v(i,j),
+// formed in FP64 from the grid and rounded once each.
 // The gradients are the reference's cell forward differences
 // (src/bathymetry/cartesian_netcdf3.rs:119-134,
 // src/current/cartesian_current.rs:515-536), so the FP32 form integrates the

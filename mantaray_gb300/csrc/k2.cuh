@@ -58,11 +58,10 @@ __device__ __forceinline__ bool locate(const PackedGrid &g, const GridPos &p, fl
   return true;
 }
 
-__device__ __forceinline__ float bilin(const float4 &v, float fx, float fy) {
-  // v = (v(i,j), v(i+1,j), v(i,j+1), v(i+1,j+1))
-  const float a = fmaf(fx, v.y - v.x, v.x);
-  const float b = fmaf(fx, v.w - v.z, v.z);
-  return fmaf(fy, b - a, a);
+// c = the cell's bilinear coefficients (batch.h): c.x + c.y fx + c.z fy +
+// c.w fx fy in three FMAs.
+__device__ __forceinline__ float bilin(const float4 &c, float fx, float fy) {
+  return fmaf(fy, fmaf(fx, c.w, c.z), fmaf(fx, c.y, c.x));
 }
 
 // The cell records a lane read last, kept in registers: a ray stays in one

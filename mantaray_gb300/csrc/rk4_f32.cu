@@ -48,6 +48,14 @@ namespace {
 
 // ---------------------------------------------------------------- K5 prep --
 
+// The bilinear of corners (v00, v10, v01, v11) as v00 + c1 fx + c2 fy +
+// c3 fx fy, the coefficients formed in FP64 and rounded once each.
+__device__ __forceinline__ float4 bilinear_coefficients(double v00, double v10, double v01,
+                                                        double v11) {
+  return make_float4(__double2float_rn(v00), __double2float_rn(v10 - v00),
+                     __double2float_rn(v01 - v00), __double2float_rn((v11 - v10) - (v01 - v00)));
+}
+
 __global__ void pack_bathy_cells(BathyDev b, float4 *cells) {
   const int64_t ncx = static_cast<int64_t>(b.nx) - 1, ncy = static_cast<int64_t>(b.ny) - 1;
   const int64_t c = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -57,8 +65,7 @@ __global__ void pack_bathy_cells(BathyDev b, float4 *cells) {
   float4 r0, r1;
   if (ne < b.depth_len) {
     const double d00 = b.depth[sw], d10 = b.depth[se], d01 = b.depth[nw], d11 = b.depth[ne];
-    r0 = make_float4(__double2float_rn(d00), __double2float_rn(d10), __double2float_rn(d01),
-                     __double2float_rn(d11));
+    r0 = bilinear_coefficients(d00, d10, d01, d11);
     r1 = make_float4(__double2float_rn((d10 - d00) / b.xspace),
                      __double2float_rn((d01 - d00) / b.yspace), 0.0f, 0.0f);
   } else {  // corners past the end of the depth array: no water
@@ -80,10 +87,8 @@ __global__ void pack_current_cells(CurrentDev cu, float4 *cells) {
   if (ne < cu.u_len && ne < cu.v_len) {
     const double u00 = cu.u[sw], u10 = cu.u[se], u01 = cu.u[nw], u11 = cu.u[ne];
     const double v00 = cu.v[sw], v10 = cu.v[se], v01 = cu.v[nw], v11 = cu.v[ne];
-    r0 = make_float4(__double2float_rn(u00), __double2float_rn(u10), __double2float_rn(u01),
-                     __double2float_rn(u11));
-    r1 = make_float4(__double2float_rn(v00), __double2float_rn(v10), __double2float_rn(v01),
-                     __double2float_rn(v11));
+    r0 = bilinear_coefficients(u00, u10, u01, u11);
+    r1 = bilinear_coefficients(v00, v10, v01, v11);
     r2 = make_float4(__double2float_rn((u10 - u00) / cu.xspace),
                      __double2float_rn((u01 - u00) / cu.yspace),
                      __double2float_rn((v10 - v00) / cu.xspace),
