@@ -44,7 +44,7 @@ OUT_BYTES_PER_ROW = 5 * 8
 # FP32 floating-point operations one ray-step of the batched kernel executes
 # (FADD/FMUL = 1, FFMA = 2), counted by ncu on the 4,096^2 shelf-slope case
 # with the current on the bathymetry's grid.
-FP32_FLOP_PER_RAY_STEP = 468.2
+FP32_FLOP_PER_RAY_STEP = 432.2
 # Algorithmic work of one ray-step (the reference's arithmetic, hand count from
 # src/wave_ray_path.rs:118-216 plus the RK4 update): ~55 FP64 add/mul/div per
 # right-hand side x 4 + ~53 for the update = 270 (36 transcendental calls not
@@ -700,7 +700,7 @@ def batched_arm(args, rank: int, world: int, local_rank: int):
     # DRAM bytes per ray-step of ncu captures (profiles/), scaled to one call's ray-steps
     k2_dram_per_ray_step = {"seamount": (18.60e6 / (65536 * 400),
                                          "65,536-ray x 400-step seamount capture"),
-                            "shelf_slope": ((460.32e6 + 44.54e6) / 330.35e6,
+                            "shelf_slope": ((450.25e6 + 43.69e6) / 330.35e6,
                                             "4,096^2-grid, 2^20-ray x 400-step shelf-slope "
                                             "capture")}
     if args.workload in k2_dram_per_ray_step:
