@@ -391,7 +391,7 @@ int mr_batch_graph_create(mr_batch *b, size_t n_max, const uint8_t *ray_scenario
   // the integrator build for this shape, chosen (an occupancy query) before
   // the capture begins
   (void)mr::rk4_f32_function(cfg->rays_per_lane, cfg->block, cfg->blocks_per_sm,
-                             b->n_scenarios);
+                             b->n_scenarios, b->host_scen[0].same_grid);
   if (e == cudaSuccess) e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
     cudaError_t le = enqueue(b, a, cfg, &gr->ord, s);
@@ -414,7 +414,8 @@ int mr_batch_graph_create(mr_batch *b, size_t n_max, const uint8_t *ray_scenario
         gr->order_node = nodes[i];
         gr->order_params = p;
       } else if (p.func == mr::rk4_f32_function(cfg->rays_per_lane, cfg->block,
-                                                cfg->blocks_per_sm, b->n_scenarios)) {
+                                                cfg->blocks_per_sm, b->n_scenarios,
+                                                b->host_scen[0].same_grid)) {
         gr->kernel_node = nodes[i];
         gr->params = p;
       }

@@ -1,8 +1,9 @@
 // k2.cuh -- the batched FP32 integrator's device code (K2), included by the
 // two translation units that instantiate its kernels: rk4_f32.cu (the
-// scenario-table builds, ONE = false) and rk4_f32_one.cu (the single-scenario
-// builds, ONE = true, compiled with FP32 subnormals flushed).  The design
-// notes are at the top of rk4_f32.cu.
+// scenario-table builds, MODE 0) and rk4_f32_one.cu (the single-scenario
+// builds, compiled with FP32 subnormals flushed: MODE 1, and MODE 2 when the
+// current is gridded on the bathymetry's grid).  The design notes are at the
+// top of rk4_f32.cu.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -88,12 +89,13 @@ struct RayLane {
   CellCache cache;
 };
 
-// Right-hand side in FP32 at offset (px, py); returns a BatchStatus.
-__device__ __forceinline__ int rhs_f32(const ScenarioDev &s, RayLane &L, float px, float py,
-                                       float kx, float ky, float d[4]) {
-  int64_t cb;
-  float fx, fy;
-  if (!locate(s.bathy, L.pb, px, py, &cb, &fx, &fy)) return BATCH_OUT_OF_DOMAIN;
+// The fields at offset (px, py) in the bathymetry cell cb (fractions fx,
+// fy), with any current: constant, gridded on the same grid, or gridded on
+// its own grid.  Returns a BatchStatus (BATCH_COMPLETE: found).
+__device__ __forceinline__ int lookup_fields(const ScenarioDev &s, RayLane &L, float px, float py,
+                                             int64_t cb, float fx, float fy, float &h, float &u,
+                                             float &v, float &dudx, float &dudy, float &dvdx,
+                                             float &dvdy) {
   CellCache &C = L.cache;
   if (cb != C.bkey) {
     C.b0 = __ldg(s.bathy.cells + 2 * cb);
@@ -102,8 +104,8 @@ __device__ __forceinline__ int rhs_f32(const ScenarioDev &s, RayLane &L, float p
     C.by = b1.y;
     C.bkey = cb;
   }
-  const float h = bilin(C.b0, fx, fy);
-  float u, v, dudx = 0.0f, dudy = 0.0f, dvdx = 0.0f, dvdy = 0.0f;
+  h = bilin(C.b0, fx, fy);
+  dudx = dudy = dvdx = dvdy = 0.0f;
   if (s.current.kind == 0) {
     int64_t cc = cb;
     float gx = fx, gy = fy;  // the same cell when the grids coincide (same origin, same arithmetic)
@@ -122,6 +124,14 @@ __device__ __forceinline__ int rhs_f32(const ScenarioDev &s, RayLane &L, float p
     u = s.current.cu;
     v = s.current.cv;
   }
+  return BATCH_COMPLETE;
+}
+
+// The ray equations in FP32 from the looked-up fields (bx, by: dh/dx,
+// dh/dy); returns a BatchStatus.
+__device__ __forceinline__ int rhs_tail(float h, float u, float v, float dudx, float dudy,
+                                        float dvdx, float dvdy, float bx, float by, float kx,
+                                        float ky, float d[4]) {
   if (!(h > 0.0f)) return h <= 0.0f ? BATCH_DRY : BATCH_OUT_OF_DOMAIN;
   const float k2 = fmaf(kx, kx, ky * ky);
   if (!(k2 > 0.0f) || !(k2 < 3.0e38f)) return BATCH_BAD_WAVENUMBER;
@@ -142,9 +152,43 @@ __device__ __forceinline__ int rhs_f32(const ScenarioDev &s, RayLane &L, float p
   const float cgk = cg * rk;            // c_g / k: c_g cos(theta) = cgk kx
   d[0] = fmaf(cgk, kx, u);
   d[1] = fmaf(cgk, ky, v);
-  d[2] = fmaf(-ky, dvdx, fmaf(-kx, dudx, f * C.bx));
-  d[3] = fmaf(-ky, dvdy, fmaf(-kx, dudy, f * C.by));
+  d[2] = fmaf(-ky, dvdx, fmaf(-kx, dudx, f * bx));
+  d[3] = fmaf(-ky, dvdy, fmaf(-kx, dudy, f * by));
   return BATCH_COMPLETE;
+}
+
+// Right-hand side in FP32 at offset (px, py); returns a BatchStatus.
+// MODE 2: the current is gridded on the bathymetry's grid, so one cell (one
+// key, one test) serves both fields; otherwise lookup_fields handles any
+// current.
+template <int MODE>
+__device__ __forceinline__ int rhs_f32(const ScenarioDev &s, RayLane &L, float px, float py,
+                                       float kx, float ky, float d[4]) {
+  int64_t cb;
+  float fx, fy;
+  if (!locate(s.bathy, L.pb, px, py, &cb, &fx, &fy)) return BATCH_OUT_OF_DOMAIN;
+  CellCache &C = L.cache;
+  float h, u, v, dudx, dudy, dvdx, dvdy;
+  if (MODE == 2) {
+    if (cb != C.bkey) {
+      C.b0 = __ldg(s.bathy.cells + 2 * cb);
+      const float4 b1 = __ldg(s.bathy.cells + 2 * cb + 1);
+      C.bx = b1.x;
+      C.by = b1.y;
+      C.c0 = __ldg(s.current.cells + 3 * cb);
+      C.c1 = __ldg(s.current.cells + 3 * cb + 1);
+      C.c2 = __ldg(s.current.cells + 3 * cb + 2);
+      C.bkey = cb;
+    }
+    h = bilin(C.b0, fx, fy);
+    u = bilin(C.c0, fx, fy);
+    v = bilin(C.c1, fx, fy);
+    dudx = C.c2.x; dudy = C.c2.y; dvdx = C.c2.z; dvdy = C.c2.w;
+  } else {
+    if (const int st = lookup_fields(s, L, px, py, cb, fx, fy, h, u, v, dudx, dudy, dvdx, dvdy))
+      return st;
+  }
+  return rhs_tail(h, u, v, dudx, dudy, dvdx, dvdy, C.bx, C.by, kx, ky, d);
 }
 
 __device__ __forceinline__ void kahan_add(float &sum, float &comp, float inc) {
@@ -193,18 +237,18 @@ __device__ __forceinline__ int32_t save_period(const BatchArgs &a) {
 }
 
 // A lane's scenario: from the kernel's parameters in the single-scenario
-// build (ONE), else from the device table.
-template <bool ONE>
+// builds (MODE 1, 2), else from the device table.
+template <int MODE>
 __device__ __forceinline__ const ScenarioDev &scenario(const BatchArgs &a, int s) {
-  return ONE ? a.scen0 : a.scen[s];
+  return MODE ? a.scen0 : a.scen[s];
 }
 
-template <bool ONE>
+template <int MODE>
 __device__ __forceinline__ void start(const BatchArgs &a, RayLane &L, int64_t r) {
   L.ray = r;
-  L.scen = (!ONE && a.ray_scenario) ? static_cast<int>(a.ray_scenario[r]) : 0;
+  L.scen = (!MODE && a.ray_scenario) ? static_cast<int>(a.ray_scenario[r]) : 0;
   if (L.scen >= a.n_scenarios) L.scen = 0;
-  const ScenarioDev &s = scenario<ONE>(a, L.scen);
+  const ScenarioDev &s = scenario<MODE>(a, L.scen);
   L.ox = a.x0[r];
   L.oy = a.y0[r];
   L.px = L.py = L.cpx = L.cpy = L.ckx = L.cky = 0.0f;
@@ -224,23 +268,23 @@ __device__ __forceinline__ void start(const BatchArgs &a, RayLane &L, int64_t r)
 }
 
 // One RK4 step of lane L.  Returns BATCH_COMPLETE while the ray goes on.
-template <bool ONE>
+template <int MODE>
 __device__ __forceinline__ int advance(const BatchArgs &a, RayLane &L) {
-  const ScenarioDev &s = scenario<ONE>(a, L.scen);
+  const ScenarioDev &s = scenario<MODE>(a, L.scen);
   // step constants in FP32 from the host (a conversion here would run on the
   // FP64 pipe, and the compiler re-derives such values under register pressure)
   const float dt = a.dt_f;
   const float half = a.half_f;
   float k1[4], k2[4], k3[4], k4[4];
-  int st = rhs_f32(s, L, L.px, L.py, L.kx, L.ky, k1);
+  int st = rhs_f32<MODE>(s, L, L.px, L.py, L.kx, L.ky, k1);
   if (st == BATCH_COMPLETE)
-    st = rhs_f32(s, L, fmaf(half, k1[0], L.px), fmaf(half, k1[1], L.py),
+    st = rhs_f32<MODE>(s, L, fmaf(half, k1[0], L.px), fmaf(half, k1[1], L.py),
                  fmaf(half, k1[2], L.kx), fmaf(half, k1[3], L.ky), k2);
   if (st == BATCH_COMPLETE)
-    st = rhs_f32(s, L, fmaf(half, k2[0], L.px), fmaf(half, k2[1], L.py),
+    st = rhs_f32<MODE>(s, L, fmaf(half, k2[0], L.px), fmaf(half, k2[1], L.py),
                  fmaf(half, k2[2], L.kx), fmaf(half, k2[3], L.ky), k3);
   if (st == BATCH_COMPLETE)
-    st = rhs_f32(s, L, fmaf(dt, k3[0], L.px), fmaf(dt, k3[1], L.py), fmaf(dt, k3[2], L.kx),
+    st = rhs_f32<MODE>(s, L, fmaf(dt, k3[0], L.px), fmaf(dt, k3[1], L.py), fmaf(dt, k3[2], L.kx),
                  fmaf(dt, k3[3], L.ky), k4);
   if (st != BATCH_COMPLETE) return st;
   const float sixth = a.sixth_f;
@@ -263,7 +307,7 @@ __device__ __forceinline__ int advance(const BatchArgs &a, RayLane &L) {
   return BATCH_COMPLETE;
 }
 
-template <int RPT, bool ONE>
+template <int RPT, int MODE>
 __device__ __forceinline__ void k2_body(const BatchArgs &a) {
   const int lane = threadIdx.x & 31;
   const unsigned lt_mask = (1u << lane) - 1u;
@@ -283,7 +327,7 @@ __device__ __forceinline__ void k2_body(const BatchArgs &a) {
         base = __shfl_sync(kFull, base, leader);
         if (L[j].ray == -1) {
           const int64_t r = static_cast<int64_t>(base) + __popc(need & lt_mask);
-          if (r < n) start<ONE>(a, L[j], a.order ? static_cast<int64_t>(__ldg(a.order + r)) : r);
+          if (r < n) start<MODE>(a, L[j], a.order ? static_cast<int64_t>(__ldg(a.order + r)) : r);
           else L[j].ray = -2;
         }
       }
@@ -299,7 +343,7 @@ __device__ __forceinline__ void k2_body(const BatchArgs &a) {
         finish(a, L[j], BATCH_COMPLETE);
         continue;
       }
-      const int st = advance<ONE>(a, L[j]);
+      const int st = advance<MODE>(a, L[j]);
       if (st != BATCH_COMPLETE) finish(a, L[j], st);
     }
   }
@@ -316,15 +360,17 @@ __device__ __forceinline__ void k2_body(const BatchArgs &a) {
 // lanes the spills only add latency (65,536-ray seamount: 22.2 -> 19.3).
 // The launcher takes the capped build when the launch asks for more blocks
 // per SM than the uncapped one holds.
-// Each has a single-scenario form (ONE: the scenario's fields are operands
-// from the kernel's parameters instead of loads at every lookup).
-template <bool ONE>
-__global__ void __launch_bounds__(256) rk4_f32_kernel_1(BatchArgs a) { k2_body<1, ONE>(a); }
-template <bool ONE>
-__global__ void __maxnreg__(72) rk4_f32_kernel_1r(BatchArgs a) { k2_body<1, ONE>(a); }
+// Each comes in three modes: 0 reads the lane's scenario from the device
+// table; 1 (one scenario) takes the scenario's fields from the kernel's
+// parameters (operands of the instructions instead of loads at every
+// lookup); 2 is mode 1 with the current gridded on the bathymetry's grid.
+template <int MODE>
+__global__ void __launch_bounds__(256) rk4_f32_kernel_1(BatchArgs a) { k2_body<1, MODE>(a); }
+template <int MODE>
+__global__ void __maxnreg__(72) rk4_f32_kernel_1r(BatchArgs a) { k2_body<1, MODE>(a); }
 // Two rays per lane hold twice the lane state: no cap.
-template <bool ONE>
-__global__ void __launch_bounds__(256) rk4_f32_kernel_2(BatchArgs a) { k2_body<2, ONE>(a); }
+template <int MODE>
+__global__ void __launch_bounds__(256) rk4_f32_kernel_2(BatchArgs a) { k2_body<2, MODE>(a); }
 
 }  // namespace
 

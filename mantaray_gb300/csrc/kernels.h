@@ -33,12 +33,14 @@ cudaError_t launch_pack_bathy(const BathyDev &b, float4 *cells, cudaStream_t str
 cudaError_t launch_pack_current(const CurrentDev &c, float4 *cells, cudaStream_t stream);
 cudaError_t launch_rk4_f32(const BatchArgs &a, int block, int blocks_per_sm, int rays_per_lane,
                            cudaStream_t stream);
-// The integrator build a launch of this shape and scenario count runs (a
-// graph's kernel node is found by it).
-const void *rk4_f32_function(int rays_per_lane, int block, int blocks_per_sm, int n_scenarios);
+// The integrator build a launch of this shape runs, for n_scenarios
+// scenarios (same_grid: the only scenario's current is gridded on its
+// bathymetry's grid); a graph's kernel node is found by it.
+const void *rk4_f32_function(int rays_per_lane, int block, int blocks_per_sm, int n_scenarios,
+                             int same_grid);
 // The single-scenario builds (rk4_f32_one.cu): 0 one ray per lane, 1 the same
 // capped at 72 registers, 2 two rays per lane.
-const void *rk4_f32_one_function(int build);
+const void *rk4_f32_one_function(int build, int same_grid);
 cudaError_t launch_fill_nan(float *p, int64_t count, cudaStream_t stream);
 
 // Spatial ordering of a batched call's rays (K6): sorts by key in `passes`

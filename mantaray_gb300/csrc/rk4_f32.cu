@@ -7,7 +7,7 @@
 // kernel, grid = SMs x blocks per SM.  Each lane holds 1 or 2 rays (_2); one
 // ray per lane has an uncapped and a 72-register build (_1r), chosen by the
 // launch shape.  Each build has a scenario-table form (instantiated here) and
-// a single-scenario form (rk4_f32_one.cu).  A lane whose ray has ended
+// two single-scenario forms (rk4_f32_one.cu).  A lane whose ray has ended
 // refills from a device work queue: the warp ballots its empty slots, one lane reserves
 // that many ray indices with a single atomicAdd and the indices are handed out
 // by rank within the ballot, so lanes never idle while work remains and rays
@@ -150,22 +150,23 @@ cudaError_t launch_fill_nan(float *p, int64_t count, cudaStream_t stream) {
 // The three builds of one form: [0] one ray per lane, uncapped; [1] the
 // same capped at 72 registers; [2] two rays per lane.
 static const void *table_builds[3] = {
-    reinterpret_cast<const void *>(&rk4_f32_kernel_1<false>),
-    reinterpret_cast<const void *>(&rk4_f32_kernel_1r<false>),
-    reinterpret_cast<const void *>(&rk4_f32_kernel_2<false>)};
+    reinterpret_cast<const void *>(&rk4_f32_kernel_1<0>),
+    reinterpret_cast<const void *>(&rk4_f32_kernel_1r<0>),
+    reinterpret_cast<const void *>(&rk4_f32_kernel_2<0>)};
 
-// Resident blocks per SM of each form's uncapped one-ray build by block
+// Resident blocks per SM of each mode's uncapped one-ray build by block
 // size (multiples of 32 up to 256), queried once; 0: not yet known.
-static std::atomic<int> g_resident_1[2][9];
+static std::atomic<int> g_resident_1[3][9];
 
-const void *rk4_f32_function(int rays_per_lane, int block, int blocks_per_sm,
-                             int n_scenarios) {
-  const int one = n_scenarios == 1 ? 1 : 0;
+const void *rk4_f32_function(int rays_per_lane, int block, int blocks_per_sm, int n_scenarios,
+                             int same_grid) {
+  const int mode = n_scenarios == 1 ? (same_grid ? 2 : 1) : 0;
   const void *fn[3];
-  for (int k = 0; k < 3; ++k) fn[k] = one ? rk4_f32_one_function(k) : table_builds[k];
+  for (int k = 0; k < 3; ++k)
+    fn[k] = mode ? rk4_f32_one_function(k, mode == 2) : table_builds[k];
   if (rays_per_lane == 2) return fn[2];
   const int slot = (block >= 32 && block <= 256 && block % 32 == 0) ? block / 32 : 0;
-  int resident = slot ? g_resident_1[one][slot].load(std::memory_order_relaxed) : 0;
+  int resident = slot ? g_resident_1[mode][slot].load(std::memory_order_relaxed) : 0;
   if (resident == 0) {
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, fn[0], block, 0) !=
             cudaSuccess ||
@@ -173,7 +174,7 @@ const void *rk4_f32_function(int rays_per_lane, int block, int blocks_per_sm,
       (void)cudaGetLastError();
       resident = blocks_per_sm;  // unknown: the uncapped build
     } else if (slot) {
-      g_resident_1[one][slot].store(resident, std::memory_order_relaxed);
+      g_resident_1[mode][slot].store(resident, std::memory_order_relaxed);
     }
   }
   return resident < blocks_per_sm ? fn[1] : fn[0];
@@ -188,7 +189,8 @@ cudaError_t launch_rk4_f32(const BatchArgs &a, int block, int blocks_per_sm, int
   if (e != cudaSuccess) return e;
   const unsigned grid = static_cast<unsigned>(sms * blocks_per_sm);
   void *args[] = {const_cast<BatchArgs *>(&a)};
-  return cudaLaunchKernel(rk4_f32_function(rays_per_lane, block, blocks_per_sm, a.n_scenarios),
+  return cudaLaunchKernel(rk4_f32_function(rays_per_lane, block, blocks_per_sm, a.n_scenarios,
+                                           a.scen0.same_grid),
                           dim3(grid), dim3(block), args, 0, stream);
 }
 

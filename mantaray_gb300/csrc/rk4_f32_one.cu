@@ -1,6 +1,7 @@
 // rk4_f32_one.cu -- the single-scenario builds of the batched FP32
-// integrator (K2, k2.cuh with ONE = true: the scenario's fields are operands
-// from the kernel's parameters).  Compiled with -ftz=true: FP32 subnormals
+// integrator (K2, k2.cuh in modes 1 and 2: the scenario's fields are
+// operands from the kernel's parameters; mode 2 when the current is gridded
+// on the bathymetry's grid).  Compiled with -ftz=true: FP32 subnormals
 // flush to zero, so the reciprocal square roots and reciprocals need no
 // subnormal handling (the 65,536-ray seamount, the shelf bump and the
 // 4,096^2 shelf-slope case ran 4-5% faster with the same endpoint errors).
@@ -14,12 +15,17 @@
 
 namespace mr {
 
-const void *rk4_f32_one_function(int build) {
+template <int MODE>
+static const void *one_build(int build) {
   switch (build) {
-    case 0: return reinterpret_cast<const void *>(&rk4_f32_kernel_1<true>);
-    case 1: return reinterpret_cast<const void *>(&rk4_f32_kernel_1r<true>);
-    default: return reinterpret_cast<const void *>(&rk4_f32_kernel_2<true>);
+    case 0: return reinterpret_cast<const void *>(&rk4_f32_kernel_1<MODE>);
+    case 1: return reinterpret_cast<const void *>(&rk4_f32_kernel_1r<MODE>);
+    default: return reinterpret_cast<const void *>(&rk4_f32_kernel_2<MODE>);
   }
+}
+
+const void *rk4_f32_one_function(int build, int same_grid) {
+  return same_grid ? one_build<2>(build) : one_build<1>(build);
 }
 
 }  // namespace mr

@@ -140,6 +140,51 @@ def test_launch_shapes_give_identical_results(mr):
                 np.testing.assert_array_equal(np.nan_to_num(a, nan=-7.0), np.nan_to_num(b_, nan=-7.0))
 
 
+@pytest.mark.parametrize("current", ["same_grid", "own_grid", "constant"])
+def test_scenario_table_and_single_scenario_builds_agree(mr, oracle, current):
+    # A one-scenario call runs a build that takes the scenario's fields from
+    # the kernel's parameters (with one cell lookup for both fields when the
+    # current is gridded on the bathymetry's grid); a call over a scenario
+    # table reads them from the table.  The same rays on the same fields,
+    # traced both ways, give the same bits; and the oracle's endpoints.
+    from mantaray_gb300.batch import BatchTracer, endpoint_errors
+    from mantaray_gb300.workloads import seamount
+
+    w = seamount(n_rays=2048, steps=300)
+    b = mr.Bathymetry.grid(w.bx, w.by, w.depth)
+    if current == "same_grid":
+        cargs = (w.cx, w.cy, w.u, w.v)
+        c = mr.Current.grid(*cargs)
+        oc = oracle.Current.grid(*cargs)
+    elif current == "own_grid":
+        # coarser than the bathymetry and offset from it
+        cx = np.arange(-500.0, 101001.0, 250.0)
+        cy = np.arange(-750.0, 101001.0, 250.0)
+        X, Y = np.meshgrid(cx, cy)
+        u = 0.3 + 0.2 * np.sin(2 * np.pi * X / 20000.0) * np.cos(2 * np.pi * Y / 30000.0)
+        v = 0.1 * np.cos(2 * np.pi * X / 25000.0)
+        c = mr.Current.grid(cx, cy, u, v)
+        oc = oracle.Current.grid(cx, cy, u, v)
+    else:
+        c = mr.Current.constant(0.3, -0.1)
+        oc = oracle.Current.constant(0.3, -0.1)
+    ax = np.array([0.0, 1000.0, 2000.0], np.float32)
+    other = (mr.Bathymetry.grid(ax, ax, np.full((3, 3), 100.0)), mr.Current.constant(0.0, 0.0))
+    x0, y0, kx0, ky0 = _dev(w.x0, w.y0, w.kx0, w.ky0)
+    (sid,) = _dev(np.zeros(w.n, np.uint8))
+    one = BatchTracer([(b, c)]).trace(x0, y0, kx0, ky0, w.dt, 300, decimation=50)
+    table = BatchTracer([(b, c), other]).trace(x0, y0, kx0, ky0, w.dt, 300, decimation=50,
+                                              scenario=sid)
+    for a, b_ in zip((one.end_state, one.n_steps, one.status, one.saved),
+                     (table.end_state, table.n_steps, table.status, table.saved)):
+        np.testing.assert_array_equal(np.nan_to_num(a.cpu().numpy(), nan=-7.0),
+                                      np.nan_to_num(b_.cpu().numpy(), nan=-7.0))
+    ob = oracle.Bathymetry.grid(w.bx, w.by, w.depth)
+    o = oracle.trace(ob, oc, w.x0, w.y0, w.kx0, w.ky0, 0.0, 300.0 * w.dt, w.dt)
+    errs = endpoint_errors(one.end_state.cpu().numpy(), one.n_steps.cpu().numpy(), o[0], o[1])
+    check_errors(errs, current)
+
+
 @pytest.mark.parametrize("order", [0, 1])
 def test_multiple_scenarios(mr, oracle, order):
     # three scenarios with different fields; each ray must see its own
