@@ -700,7 +700,7 @@ def batched_arm(args, rank: int, world: int, local_rank: int):
     # DRAM bytes per ray-step of ncu captures (profiles/), scaled to one call's ray-steps
     k2_dram_per_ray_step = {"seamount": (18.60e6 / (65536 * 400),
                                          "65,536-ray x 400-step seamount capture"),
-                            "shelf_slope": ((450.25e6 + 43.69e6) / 330.35e6,
+                            "shelf_slope": ((452.10e6 + 36.66e6) / 330.35e6,
                                             "4,096^2-grid, 2^20-ray x 400-step shelf-slope "
                                             "capture")}
     if args.workload in k2_dram_per_ray_step:
