@@ -53,6 +53,7 @@ struct BatchArgs {
   const ScenarioDev *scen;   // [n_scenarios]
   ScenarioDev scen0;         // scen[0] by value: the single-scenario build reads it from
                              // the kernel's parameters, with no load
+  int all_same_grid;         // every scenario's current is gridded on its bathymetry's grid
   int n_scenarios;
   const uint8_t *ray_scenario;  // [n] scenario per ray, or null (all scenario 0)
   int64_t n;                 // rays of this call

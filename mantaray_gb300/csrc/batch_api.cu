@@ -204,6 +204,7 @@ int fill_args(mr_batch *b, size_t n, size_t n_stride, const uint8_t *ray_scenari
   if (!(dt > 0.0) || !isfinite(t0)) return fail(MR_ERR_INVALID_ARGUMENT, "dt must be > 0");
   a->scen = b->scen;
   a->scen0 = b->host_scen[0];
+  a->all_same_grid = all_same_grid(b);
   a->n_scenarios = b->n_scenarios;
   a->ray_scenario = ray_scenario;
   a->n = static_cast<int64_t>(n);
@@ -391,7 +392,7 @@ int mr_batch_graph_create(mr_batch *b, size_t n_max, const uint8_t *ray_scenario
   // the integrator build for this shape, chosen (an occupancy query) before
   // the capture begins
   (void)mr::rk4_f32_function(cfg->rays_per_lane, cfg->block, cfg->blocks_per_sm,
-                             b->n_scenarios, b->host_scen[0].same_grid);
+                             b->n_scenarios, all_same_grid(b));
   if (e == cudaSuccess) e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
     cudaError_t le = enqueue(b, a, cfg, &gr->ord, s);
@@ -415,7 +416,7 @@ int mr_batch_graph_create(mr_batch *b, size_t n_max, const uint8_t *ray_scenario
         gr->order_params = p;
       } else if (p.func == mr::rk4_f32_function(cfg->rays_per_lane, cfg->block,
                                                 cfg->blocks_per_sm, b->n_scenarios,
-                                                b->host_scen[0].same_grid)) {
+                                                all_same_grid(b))) {
         gr->kernel_node = nodes[i];
         gr->params = p;
       }

@@ -31,3 +31,11 @@ struct mr_batch {
   int order_scen_shift = 8;          // key layout of the ordering (order.cu)
   int order_passes = 1;
 };
+
+// 1 when every scenario's current is gridded on its bathymetry's grid (the
+// batched kernel then takes one cell lookup for both fields).
+inline int all_same_grid(const mr_batch *b) {
+  for (const auto &sc : b->host_scen)
+    if (!sc.same_grid) return 0;
+  return 1;
+}

@@ -105,6 +105,7 @@ extern "C" int mr_batch_trace_device_static(
   mr::BatchArgs a{};
   a.scen = table;
   a.scen0 = b->host_scen[0];
+  a.all_same_grid = all_same_grid(b);
   a.n_scenarios = b->n_scenarios;
   a.ray_scenario = ray_scenario;
   a.n = static_cast<int64_t>(n);

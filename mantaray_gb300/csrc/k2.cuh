@@ -1,6 +1,7 @@
 // k2.cuh -- the batched FP32 integrator's device code (K2), included by the
 // two translation units that instantiate its kernels: rk4_f32.cu (the
-// scenario-table builds, MODE 0) and rk4_f32_one.cu (the single-scenario
+// scenario-table builds: MODE 0, and MODE 3 when every scenario's current is
+// gridded on its bathymetry's grid) and rk4_f32_one.cu (the single-scenario
 // builds, compiled with FP32 subnormals flushed: MODE 1, and MODE 2 when the
 // current is gridded on the bathymetry's grid).  The design notes are at the
 // top of rk4_f32.cu.
@@ -158,9 +159,9 @@ __device__ __forceinline__ int rhs_tail(float h, float u, float v, float dudx, f
 }
 
 // Right-hand side in FP32 at offset (px, py); returns a BatchStatus.
-// MODE 2: the current is gridded on the bathymetry's grid, so one cell (one
-// key, one test) serves both fields; otherwise lookup_fields handles any
-// current.
+// MODE 2 and 3: the current is gridded on the bathymetry's grid, so one cell
+// (one key, one test) serves both fields; otherwise lookup_fields handles
+// any current.
 template <int MODE>
 __device__ __forceinline__ int rhs_f32(const ScenarioDev &s, RayLane &L, float px, float py,
                                        float kx, float ky, float d[4]) {
@@ -169,7 +170,7 @@ __device__ __forceinline__ int rhs_f32(const ScenarioDev &s, RayLane &L, float p
   if (!locate(s.bathy, L.pb, px, py, &cb, &fx, &fy)) return BATCH_OUT_OF_DOMAIN;
   CellCache &C = L.cache;
   float h, u, v, dudx, dudy, dvdx, dvdy;
-  if (MODE == 2) {
+  if (MODE == 2 || MODE == 3) {
     if (cb != C.bkey) {
       C.b0 = __ldg(s.bathy.cells + 2 * cb);
       const float4 b1 = __ldg(s.bathy.cells + 2 * cb + 1);
@@ -237,16 +238,17 @@ __device__ __forceinline__ int32_t save_period(const BatchArgs &a) {
 }
 
 // A lane's scenario: from the kernel's parameters in the single-scenario
-// builds (MODE 1, 2), else from the device table.
+// builds (MODE 1, 2), else from the device table (MODE 0, 3).
 template <int MODE>
 __device__ __forceinline__ const ScenarioDev &scenario(const BatchArgs &a, int s) {
-  return MODE ? a.scen0 : a.scen[s];
+  return (MODE == 1 || MODE == 2) ? a.scen0 : a.scen[s];
 }
 
 template <int MODE>
 __device__ __forceinline__ void start(const BatchArgs &a, RayLane &L, int64_t r) {
   L.ray = r;
-  L.scen = (!MODE && a.ray_scenario) ? static_cast<int>(a.ray_scenario[r]) : 0;
+  L.scen = ((MODE == 0 || MODE == 3) && a.ray_scenario) ? static_cast<int>(a.ray_scenario[r])
+                                                         : 0;
   if (L.scen >= a.n_scenarios) L.scen = 0;
   const ScenarioDev &s = scenario<MODE>(a, L.scen);
   L.ox = a.x0[r];
@@ -360,10 +362,11 @@ __device__ __forceinline__ void k2_body(const BatchArgs &a) {
 // lanes the spills only add latency (65,536-ray seamount: 22.2 -> 19.3).
 // The launcher takes the capped build when the launch asks for more blocks
 // per SM than the uncapped one holds.
-// Each comes in three modes: 0 reads the lane's scenario from the device
+// Each comes in four modes: 0 reads the lane's scenario from the device
 // table; 1 (one scenario) takes the scenario's fields from the kernel's
 // parameters (operands of the instructions instead of loads at every
-// lookup); 2 is mode 1 with the current gridded on the bathymetry's grid.
+// lookup); 2 is mode 1 and 3 is mode 0 with the current gridded on the
+// bathymetry's grid (every scenario's, for 3).
 template <int MODE>
 __global__ void __launch_bounds__(256) rk4_f32_kernel_1(BatchArgs a) { k2_body<1, MODE>(a); }
 template <int MODE>

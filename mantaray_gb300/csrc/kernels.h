@@ -34,7 +34,7 @@ cudaError_t launch_pack_current(const CurrentDev &c, float4 *cells, cudaStream_t
 cudaError_t launch_rk4_f32(const BatchArgs &a, int block, int blocks_per_sm, int rays_per_lane,
                            cudaStream_t stream);
 // The integrator build a launch of this shape runs, for n_scenarios
-// scenarios (same_grid: the only scenario's current is gridded on its
+// scenarios (same_grid: every scenario's current is gridded on its
 // bathymetry's grid); a graph's kernel node is found by it.
 const void *rk4_f32_function(int rays_per_lane, int block, int blocks_per_sm, int n_scenarios,
                              int same_grid);

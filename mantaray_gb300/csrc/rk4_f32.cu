@@ -6,8 +6,8 @@
 // K2 (rk4_f32_kernel_1 / _1r / _2, device code in k2.cuh): a persistent
 // kernel, grid = SMs x blocks per SM.  Each lane holds 1 or 2 rays (_2); one
 // ray per lane has an uncapped and a 72-register build (_1r), chosen by the
-// launch shape.  Each build has a scenario-table form (instantiated here) and
-// two single-scenario forms (rk4_f32_one.cu).  A lane whose ray has ended
+// launch shape.  Each build has two scenario-table forms (instantiated here)
+// and two single-scenario forms (rk4_f32_one.cu).  A lane whose ray has ended
 // refills from a device work queue: the warp ballots its empty slots, one lane reserves
 // that many ray indices with a single atomicAdd and the indices are handed out
 // by rank within the ballot, so lanes never idle while work remains and rays
@@ -147,23 +147,28 @@ cudaError_t launch_fill_nan(float *p, int64_t count, cudaStream_t stream) {
   return cudaGetLastError();
 }
 
-// The three builds of one form: [0] one ray per lane, uncapped; [1] the
-// same capped at 72 registers; [2] two rays per lane.
-static const void *table_builds[3] = {
-    reinterpret_cast<const void *>(&rk4_f32_kernel_1<0>),
-    reinterpret_cast<const void *>(&rk4_f32_kernel_1r<0>),
-    reinterpret_cast<const void *>(&rk4_f32_kernel_2<0>)};
+// The three builds of each table mode: [0] one ray per lane, uncapped; [1]
+// the same capped at 72 registers; [2] two rays per lane.  Row 0: mode 0,
+// row 1: mode 3 (every current on its bathymetry's grid).
+static const void *table_builds[2][3] = {
+    {reinterpret_cast<const void *>(&rk4_f32_kernel_1<0>),
+     reinterpret_cast<const void *>(&rk4_f32_kernel_1r<0>),
+     reinterpret_cast<const void *>(&rk4_f32_kernel_2<0>)},
+    {reinterpret_cast<const void *>(&rk4_f32_kernel_1<3>),
+     reinterpret_cast<const void *>(&rk4_f32_kernel_1r<3>),
+     reinterpret_cast<const void *>(&rk4_f32_kernel_2<3>)}};
 
 // Resident blocks per SM of each mode's uncapped one-ray build by block
 // size (multiples of 32 up to 256), queried once; 0: not yet known.
-static std::atomic<int> g_resident_1[3][9];
+static std::atomic<int> g_resident_1[4][9];
 
 const void *rk4_f32_function(int rays_per_lane, int block, int blocks_per_sm, int n_scenarios,
                              int same_grid) {
-  const int mode = n_scenarios == 1 ? (same_grid ? 2 : 1) : 0;
+  const int mode = n_scenarios == 1 ? (same_grid ? 2 : 1) : (same_grid ? 3 : 0);
   const void *fn[3];
   for (int k = 0; k < 3; ++k)
-    fn[k] = mode ? rk4_f32_one_function(k, mode == 2) : table_builds[k];
+    fn[k] = (mode == 1 || mode == 2) ? rk4_f32_one_function(k, mode == 2)
+                                     : table_builds[mode == 3][k];
   if (rays_per_lane == 2) return fn[2];
   const int slot = (block >= 32 && block <= 256 && block % 32 == 0) ? block / 32 : 0;
   int resident = slot ? g_resident_1[mode][slot].load(std::memory_order_relaxed) : 0;
@@ -190,7 +195,7 @@ cudaError_t launch_rk4_f32(const BatchArgs &a, int block, int blocks_per_sm, int
   const unsigned grid = static_cast<unsigned>(sms * blocks_per_sm);
   void *args[] = {const_cast<BatchArgs *>(&a)};
   return cudaLaunchKernel(rk4_f32_function(rays_per_lane, block, blocks_per_sm, a.n_scenarios,
-                                           a.scen0.same_grid),
+                                           a.all_same_grid),
                           dim3(grid), dim3(block), args, 0, stream);
 }
 

@@ -168,8 +168,14 @@ def test_scenario_table_and_single_scenario_builds_agree(mr, oracle, current):
     else:
         c = mr.Current.constant(0.3, -0.1)
         oc = oracle.Current.constant(0.3, -0.1)
+    # a second scenario for the table: with the current on its bathymetry's
+    # grid too when the first has it (the table build that takes one cell
+    # for both fields), else a constant current (the general table build)
     ax = np.array([0.0, 1000.0, 2000.0], np.float32)
-    other = (mr.Bathymetry.grid(ax, ax, np.full((3, 3), 100.0)), mr.Current.constant(0.0, 0.0))
+    oc2 = (mr.Current.grid(ax.astype(np.float64), ax.astype(np.float64), np.zeros((3, 3)),
+                           np.zeros((3, 3))) if current == "same_grid"
+           else mr.Current.constant(0.0, 0.0))
+    other = (mr.Bathymetry.grid(ax, ax, np.full((3, 3), 100.0)), oc2)
     x0, y0, kx0, ky0 = _dev(w.x0, w.y0, w.kx0, w.ky0)
     (sid,) = _dev(np.zeros(w.n, np.uint8))
     one = BatchTracer([(b, c)]).trace(x0, y0, kx0, ky0, w.dt, 300, decimation=50)
