@@ -62,6 +62,24 @@ __device__ __forceinline__ bool locate(const PackedGrid &g, const GridPos &p, fl
 
 // c = the cell's bilinear coefficients (batch.h): c.x + c.y fx + c.z fy +
 // c.w fx fy in three FMAs.
+// locate for the branch-free right-hand side: the same cell and fractions
+// inside the grid; outside it (or at a NaN position) returns false with the
+// cell clamped into the grid, so that its record can be read all the same.
+__device__ __forceinline__ bool locate_clamped(const PackedGrid &g, const GridPos &p, float px,
+                                               float py, int64_t *cell, float *fx, float *fy) {
+  const float ux = fmaf(px, g.inv_sp_x, p.f0);
+  const float uy = fmaf(py, g.inv_sp_y, p.g0);
+  const float flx = floorf(ux), fly = floorf(uy);
+  const float cx = p.fi0 + flx, cy = p.fj0 + fly;
+  const bool inside = cx >= 0.0f && cx <= g.cx_max && cy >= 0.0f && cy <= g.cy_max;
+  // fmaxf(NaN, 0) is 0: a NaN coordinate clamps too
+  const float kx = fminf(fmaxf(cx, 0.0f), g.cx_max), ky = fminf(fmaxf(cy, 0.0f), g.cy_max);
+  *cell = static_cast<int64_t>(static_cast<int>(ky)) * (g.nx - 1) + static_cast<int>(kx);
+  *fx = ux - flx;
+  *fy = uy - fly;
+  return inside;
+}
+
 __device__ __forceinline__ float bilin(const float4 &c, float fx, float fy) {
   return fmaf(fy, fmaf(fx, c.w, c.z), fmaf(fx, c.y, c.x));
 }
@@ -156,6 +174,62 @@ __device__ __forceinline__ int rhs_tail(float h, float u, float v, float dudx, f
   d[2] = fmaf(-ky, dvdx, fmaf(-kx, dudx, f * bx));
   d[3] = fmaf(-ky, dvdy, fmaf(-kx, dudy, f * by));
   return BATCH_COMPLETE;
+}
+
+// rhs_tail without early returns: d is always written (meaningless when the
+// status is not BATCH_COMPLETE); st is the status so far.
+__device__ __forceinline__ int rhs_tail_flat(int st, float h, float u, float v, float dudx,
+                                             float dudy, float dvdx, float dvdy, float bx,
+                                             float by, float kx, float ky, float d[4]) {
+  if (st == BATCH_COMPLETE && !(h > 0.0f)) st = h <= 0.0f ? BATCH_DRY : BATCH_OUT_OF_DOMAIN;
+  const float k2 = fmaf(kx, kx, ky * ky);
+  if (st == BATCH_COMPLETE && !(k2 > 0.0f && k2 < 3.0e38f)) st = BATCH_BAD_WAVENUMBER;
+  const float rk = rsqrtf(k2);
+  const float k = k2 * rk;
+  const float kh = k * h;
+  const float m = -expm1f(-2.0f * kh);  // 1 - exp(-2kh)
+  const float q = 1.0f - m;
+  const float inv_d = __frcp_rn(m * (2.0f - m));  // = 1.0f / x, correctly rounded
+  const float r = m * inv_d;            // 1 / (2 - m)
+  const float th = m * r;               // tanh(kh)
+  const float gkt = kGf * k * th;
+  const float rs = rsqrtf(gkt);
+  const float q4 = 4.0f * q;
+  const float cg = (0.5f * kGf) * (fmaf(kh * q4, r * r, th) * rs);
+  const float f = (-0.5f * k) * ((q4 * inv_d) * (gkt * rs));
+  const float cgk = cg * rk;
+  d[0] = fmaf(cgk, kx, u);
+  d[1] = fmaf(cgk, ky, v);
+  d[2] = fmaf(-ky, dvdx, fmaf(-kx, dudx, f * bx));
+  d[3] = fmaf(-ky, dvdy, fmaf(-kx, dudy, f * by));
+  return st;
+}
+
+// Right-hand side of modes 2 and 3 (current gridded on the bathymetry's
+// grid) without early returns: the same values and statuses as rhs_f32, with
+// d always written, so that the four stages of a step need no branches
+// between them.  Only the cell-record load is conditional.
+__device__ __forceinline__ int rhs_f32_flat(const ScenarioDev &s, RayLane &L, float px, float py,
+                                            float kx, float ky, float d[4]) {
+  int64_t cb;
+  float fx, fy;
+  const bool inside = locate_clamped(s.bathy, L.pb, px, py, &cb, &fx, &fy);
+  CellCache &C = L.cache;
+  if (cb != C.bkey) {
+    C.b0 = __ldg(s.bathy.cells + 2 * cb);
+    const float4 b1 = __ldg(s.bathy.cells + 2 * cb + 1);
+    C.bx = b1.x;
+    C.by = b1.y;
+    C.c0 = __ldg(s.current.cells + 3 * cb);
+    C.c1 = __ldg(s.current.cells + 3 * cb + 1);
+    C.c2 = __ldg(s.current.cells + 3 * cb + 2);
+    C.bkey = cb;
+  }
+  const float h = bilin(C.b0, fx, fy);
+  const float u = bilin(C.c0, fx, fy);
+  const float v = bilin(C.c1, fx, fy);
+  return rhs_tail_flat(inside ? BATCH_COMPLETE : BATCH_OUT_OF_DOMAIN, h, u, v, C.c2.x, C.c2.y,
+                       C.c2.z, C.c2.w, C.bx, C.by, kx, ky, d);
 }
 
 // Right-hand side in FP32 at offset (px, py); returns a BatchStatus.
@@ -270,7 +344,11 @@ __device__ __forceinline__ void start(const BatchArgs &a, RayLane &L, int64_t r)
 }
 
 // One RK4 step of lane L.  Returns BATCH_COMPLETE while the ray goes on.
-template <int MODE>
+// FLAT (modes 2 and 3 only): the four stages without branches between them
+// (rhs_f32_flat), which needs more registers: the uncapped build takes it
+// (65,536-ray seamount 33.6 -> 35.7 G ray-steps/s), the 72-register build
+// does not (it spilled: 4,096^2 shelf-slope 50.1 -> 47.3 G).
+template <int MODE, bool FLAT>
 __device__ __forceinline__ int advance(const BatchArgs &a, RayLane &L) {
   const ScenarioDev &s = scenario<MODE>(a, L.scen);
   // step constants in FP32 from the host (a conversion here would run on the
@@ -278,16 +356,30 @@ __device__ __forceinline__ int advance(const BatchArgs &a, RayLane &L) {
   const float dt = a.dt_f;
   const float half = a.half_f;
   float k1[4], k2[4], k3[4], k4[4];
-  int st = rhs_f32<MODE>(s, L, L.px, L.py, L.kx, L.ky, k1);
-  if (st == BATCH_COMPLETE)
-    st = rhs_f32<MODE>(s, L, fmaf(half, k1[0], L.px), fmaf(half, k1[1], L.py),
-                 fmaf(half, k1[2], L.kx), fmaf(half, k1[3], L.ky), k2);
-  if (st == BATCH_COMPLETE)
-    st = rhs_f32<MODE>(s, L, fmaf(half, k2[0], L.px), fmaf(half, k2[1], L.py),
-                 fmaf(half, k2[2], L.kx), fmaf(half, k2[3], L.ky), k3);
-  if (st == BATCH_COMPLETE)
-    st = rhs_f32<MODE>(s, L, fmaf(dt, k3[0], L.px), fmaf(dt, k3[1], L.py), fmaf(dt, k3[2], L.kx),
-                 fmaf(dt, k3[3], L.ky), k4);
+  int st;
+  if (FLAT && (MODE == 2 || MODE == 3)) {
+    // all four stages, then the first stage's failure (a failed stage's
+    // derivative only feeds stages whose results are dropped)
+    st = rhs_f32_flat(s, L, L.px, L.py, L.kx, L.ky, k1);
+    const int s2 = rhs_f32_flat(s, L, fmaf(half, k1[0], L.px), fmaf(half, k1[1], L.py),
+                                fmaf(half, k1[2], L.kx), fmaf(half, k1[3], L.ky), k2);
+    const int s3 = rhs_f32_flat(s, L, fmaf(half, k2[0], L.px), fmaf(half, k2[1], L.py),
+                                fmaf(half, k2[2], L.kx), fmaf(half, k2[3], L.ky), k3);
+    const int s4 = rhs_f32_flat(s, L, fmaf(dt, k3[0], L.px), fmaf(dt, k3[1], L.py),
+                                fmaf(dt, k3[2], L.kx), fmaf(dt, k3[3], L.ky), k4);
+    st = st != BATCH_COMPLETE ? st : s2 != BATCH_COMPLETE ? s2 : s3 != BATCH_COMPLETE ? s3 : s4;
+  } else {
+    st = rhs_f32<MODE>(s, L, L.px, L.py, L.kx, L.ky, k1);
+    if (st == BATCH_COMPLETE)
+      st = rhs_f32<MODE>(s, L, fmaf(half, k1[0], L.px), fmaf(half, k1[1], L.py),
+                         fmaf(half, k1[2], L.kx), fmaf(half, k1[3], L.ky), k2);
+    if (st == BATCH_COMPLETE)
+      st = rhs_f32<MODE>(s, L, fmaf(half, k2[0], L.px), fmaf(half, k2[1], L.py),
+                         fmaf(half, k2[2], L.kx), fmaf(half, k2[3], L.ky), k3);
+    if (st == BATCH_COMPLETE)
+      st = rhs_f32<MODE>(s, L, fmaf(dt, k3[0], L.px), fmaf(dt, k3[1], L.py),
+                         fmaf(dt, k3[2], L.kx), fmaf(dt, k3[3], L.ky), k4);
+  }
   if (st != BATCH_COMPLETE) return st;
   const float sixth = a.sixth_f;
 #pragma unroll
@@ -309,7 +401,7 @@ __device__ __forceinline__ int advance(const BatchArgs &a, RayLane &L) {
   return BATCH_COMPLETE;
 }
 
-template <int RPT, int MODE>
+template <int RPT, int MODE, bool FLAT>
 __device__ __forceinline__ void k2_body(const BatchArgs &a) {
   const int lane = threadIdx.x & 31;
   const unsigned lt_mask = (1u << lane) - 1u;
@@ -345,7 +437,7 @@ __device__ __forceinline__ void k2_body(const BatchArgs &a) {
         finish(a, L[j], BATCH_COMPLETE);
         continue;
       }
-      const int st = advance<MODE>(a, L[j]);
+      const int st = advance<MODE, FLAT>(a, L[j]);
       if (st != BATCH_COMPLETE) finish(a, L[j], st);
     }
   }
@@ -368,12 +460,14 @@ __device__ __forceinline__ void k2_body(const BatchArgs &a) {
 // lookup); 2 is mode 1 and 3 is mode 0 with the current gridded on the
 // bathymetry's grid (every scenario's, for 3).
 template <int MODE>
-__global__ void __launch_bounds__(256) rk4_f32_kernel_1(BatchArgs a) { k2_body<1, MODE>(a); }
+__global__ void __launch_bounds__(256) rk4_f32_kernel_1(BatchArgs a) {
+  k2_body<1, MODE, true>(a);
+}
 template <int MODE>
-__global__ void __maxnreg__(72) rk4_f32_kernel_1r(BatchArgs a) { k2_body<1, MODE>(a); }
+__global__ void __maxnreg__(72) rk4_f32_kernel_1r(BatchArgs a) { k2_body<1, MODE, false>(a); }
 // Two rays per lane hold twice the lane state: no cap.
 template <int MODE>
-__global__ void __launch_bounds__(256) rk4_f32_kernel_2(BatchArgs a) { k2_body<2, MODE>(a); }
+__global__ void __launch_bounds__(256) rk4_f32_kernel_2(BatchArgs a) { k2_body<2, MODE, false>(a); }
 
 }  // namespace
 
