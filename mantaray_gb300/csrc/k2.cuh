@@ -147,13 +147,11 @@ __device__ __forceinline__ int lookup_fields(const ScenarioDev &s, RayLane &L, f
 }
 
 // The ray equations in FP32 from the looked-up fields (bx, by: dh/dx,
-// dh/dy); returns a BatchStatus.
-__device__ __forceinline__ int rhs_tail(float h, float u, float v, float dudx, float dudy,
-                                        float dvdx, float dvdy, float bx, float by, float kx,
-                                        float ky, float d[4]) {
-  if (!(h > 0.0f)) return h <= 0.0f ? BATCH_DRY : BATCH_OUT_OF_DOMAIN;
+// dh/dy): the identity form of the right-hand side in single precision.
+__device__ __forceinline__ void ray_equations(float h, float u, float v, float dudx, float dudy,
+                                              float dvdx, float dvdy, float bx, float by,
+                                              float kx, float ky, float d[4]) {
   const float k2 = fmaf(kx, kx, ky * ky);
-  if (!(k2 > 0.0f) || !(k2 < 3.0e38f)) return BATCH_BAD_WAVENUMBER;
   const float rk = rsqrtf(k2);
   const float k = k2 * rk;
   const float kh = k * h;
@@ -173,48 +171,22 @@ __device__ __forceinline__ int rhs_tail(float h, float u, float v, float dudx, f
   d[1] = fmaf(cgk, ky, v);
   d[2] = fmaf(-ky, dvdx, fmaf(-kx, dudx, f * bx));
   d[3] = fmaf(-ky, dvdy, fmaf(-kx, dudy, f * by));
+}
+
+// The status of a right-hand side from the looked-up depth and the
+// wavenumber: dry (h <= 0), out of domain (h NaN: a cell past the depth
+// array), bad wavenumber (k^2 not in (0, 3e38)), else complete.
+__device__ __forceinline__ int field_status(float h, float kx, float ky) {
+  if (!(h > 0.0f)) return h <= 0.0f ? BATCH_DRY : BATCH_OUT_OF_DOMAIN;
+  const float k2 = fmaf(kx, kx, ky * ky);
+  if (!(k2 > 0.0f && k2 < 3.0e38f)) return BATCH_BAD_WAVENUMBER;
   return BATCH_COMPLETE;
 }
 
-// rhs_tail without early returns: d is always written (meaningless when the
-// status is not BATCH_COMPLETE); st is the status so far.
-__device__ __forceinline__ int rhs_tail_flat(int st, float h, float u, float v, float dudx,
-                                             float dudy, float dvdx, float dvdy, float bx,
-                                             float by, float kx, float ky, float d[4]) {
-  if (st == BATCH_COMPLETE && !(h > 0.0f)) st = h <= 0.0f ? BATCH_DRY : BATCH_OUT_OF_DOMAIN;
-  const float k2 = fmaf(kx, kx, ky * ky);
-  if (st == BATCH_COMPLETE && !(k2 > 0.0f && k2 < 3.0e38f)) st = BATCH_BAD_WAVENUMBER;
-  const float rk = rsqrtf(k2);
-  const float k = k2 * rk;
-  const float kh = k * h;
-  const float m = -expm1f(-2.0f * kh);  // 1 - exp(-2kh)
-  const float q = 1.0f - m;
-  const float inv_d = __frcp_rn(m * (2.0f - m));  // = 1.0f / x, correctly rounded
-  const float r = m * inv_d;            // 1 / (2 - m)
-  const float th = m * r;               // tanh(kh)
-  const float gkt = kGf * k * th;
-  const float rs = rsqrtf(gkt);
-  const float q4 = 4.0f * q;
-  const float cg = (0.5f * kGf) * (fmaf(kh * q4, r * r, th) * rs);
-  const float f = (-0.5f * k) * ((q4 * inv_d) * (gkt * rs));
-  const float cgk = cg * rk;
-  d[0] = fmaf(cgk, kx, u);
-  d[1] = fmaf(cgk, ky, v);
-  d[2] = fmaf(-ky, dvdx, fmaf(-kx, dudx, f * bx));
-  d[3] = fmaf(-ky, dvdy, fmaf(-kx, dudy, f * by));
-  return st;
-}
-
-// Right-hand side of modes 2 and 3 (current gridded on the bathymetry's
-// grid) without early returns: the same values and statuses as rhs_f32, with
-// d always written, so that the four stages of a step need no branches
-// between them.  Only the cell-record load is conditional.
-__device__ __forceinline__ int rhs_f32_flat(const ScenarioDev &s, RayLane &L, float px, float py,
-                                            float kx, float ky, float d[4]) {
-  int64_t cb;
-  float fx, fy;
-  const bool inside = locate_clamped(s.bathy, L.pb, px, py, &cb, &fx, &fy);
-  CellCache &C = L.cache;
+// The record of cell cb of both fields when the current is gridded on the
+// bathymetry's grid (modes 2 and 3), unless the lane holds it already.
+__device__ __forceinline__ void load_same_grid_cell(const ScenarioDev &s, CellCache &C,
+                                                    int64_t cb) {
   if (cb != C.bkey) {
     C.b0 = __ldg(s.bathy.cells + 2 * cb);
     const float4 b1 = __ldg(s.bathy.cells + 2 * cb + 1);
@@ -225,11 +197,24 @@ __device__ __forceinline__ int rhs_f32_flat(const ScenarioDev &s, RayLane &L, fl
     C.c2 = __ldg(s.current.cells + 3 * cb + 2);
     C.bkey = cb;
   }
+}
+
+// Right-hand side of modes 2 and 3 without early returns: the same values
+// and statuses as rhs_f32, with d always written (meaningless unless the
+// status is BATCH_COMPLETE), so that the four stages of a step need no
+// branches between them.  Only the cell-record load is conditional.
+__device__ __forceinline__ int rhs_f32_flat(const ScenarioDev &s, RayLane &L, float px, float py,
+                                            float kx, float ky, float d[4]) {
+  int64_t cb;
+  float fx, fy;
+  const bool inside = locate_clamped(s.bathy, L.pb, px, py, &cb, &fx, &fy);
+  CellCache &C = L.cache;
+  load_same_grid_cell(s, C, cb);
   const float h = bilin(C.b0, fx, fy);
-  const float u = bilin(C.c0, fx, fy);
-  const float v = bilin(C.c1, fx, fy);
-  return rhs_tail_flat(inside ? BATCH_COMPLETE : BATCH_OUT_OF_DOMAIN, h, u, v, C.c2.x, C.c2.y,
-                       C.c2.z, C.c2.w, C.bx, C.by, kx, ky, d);
+  const int st = inside ? field_status(h, kx, ky) : BATCH_OUT_OF_DOMAIN;
+  ray_equations(h, bilin(C.c0, fx, fy), bilin(C.c1, fx, fy), C.c2.x, C.c2.y, C.c2.z, C.c2.w,
+                C.bx, C.by, kx, ky, d);
+  return st;
 }
 
 // Right-hand side in FP32 at offset (px, py); returns a BatchStatus.
@@ -245,16 +230,7 @@ __device__ __forceinline__ int rhs_f32(const ScenarioDev &s, RayLane &L, float p
   CellCache &C = L.cache;
   float h, u, v, dudx, dudy, dvdx, dvdy;
   if (MODE == 2 || MODE == 3) {
-    if (cb != C.bkey) {
-      C.b0 = __ldg(s.bathy.cells + 2 * cb);
-      const float4 b1 = __ldg(s.bathy.cells + 2 * cb + 1);
-      C.bx = b1.x;
-      C.by = b1.y;
-      C.c0 = __ldg(s.current.cells + 3 * cb);
-      C.c1 = __ldg(s.current.cells + 3 * cb + 1);
-      C.c2 = __ldg(s.current.cells + 3 * cb + 2);
-      C.bkey = cb;
-    }
+    load_same_grid_cell(s, C, cb);
     h = bilin(C.b0, fx, fy);
     u = bilin(C.c0, fx, fy);
     v = bilin(C.c1, fx, fy);
@@ -263,7 +239,9 @@ __device__ __forceinline__ int rhs_f32(const ScenarioDev &s, RayLane &L, float p
     if (const int st = lookup_fields(s, L, px, py, cb, fx, fy, h, u, v, dudx, dudy, dvdx, dvdy))
       return st;
   }
-  return rhs_tail(h, u, v, dudx, dudy, dvdx, dvdy, C.bx, C.by, kx, ky, d);
+  if (const int st = field_status(h, kx, ky)) return st;
+  ray_equations(h, u, v, dudx, dudy, dvdx, dvdy, C.bx, C.by, kx, ky, d);
+  return BATCH_COMPLETE;
 }
 
 __device__ __forceinline__ void kahan_add(float &sum, float &comp, float inc) {
