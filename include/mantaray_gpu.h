@@ -197,7 +197,9 @@ typedef struct mr_batch_graph mr_batch_graph;
 /* Launch shape of the persistent kernel. */
 typedef struct mr_batch_config {
   int block;           /* threads per block: a multiple of 32 in [32, 256] */
-  int blocks_per_sm;   /* resident blocks per SM of the persistent grid */
+  int blocks_per_sm;   /* blocks per SM of the persistent grid; with one ray per
+                          lane, more than the kernel's register-hungry build
+                          holds selects its 72-register build (same results) */
   int rays_per_lane;   /* 1 or 2 rays interleaved per thread */
   int rebase_interval; /* steps between FP64 origin rebases */
   int order;           /* 1: sort the rays by starting cell and direction before
