@@ -60,8 +60,6 @@ __device__ __forceinline__ bool locate(const PackedGrid &g, const GridPos &p, fl
   return true;
 }
 
-// c = the cell's bilinear coefficients (batch.h): c.x + c.y fx + c.z fy +
-// c.w fx fy in three FMAs.
 // locate for the branch-free right-hand side: the same cell and fractions
 // inside the grid; outside it (or at a NaN position) returns false with the
 // cell clamped into the grid, so that its record can be read all the same.
@@ -80,6 +78,8 @@ __device__ __forceinline__ bool locate_clamped(const PackedGrid &g, const GridPo
   return inside;
 }
 
+// c = the cell's bilinear coefficients (batch.h): c.x + c.y fx + c.z fy +
+// c.w fx fy in three FMAs.
 __device__ __forceinline__ float bilin(const float4 &c, float fx, float fy) {
   return fmaf(fy, fmaf(fx, c.w, c.z), fmaf(fx, c.y, c.x));
 }
@@ -89,9 +89,9 @@ __device__ __forceinline__ float bilin(const float4 &c, float fx, float fy) {
 // loading them again (same values, no memory latency on the dependent chain).
 struct CellCache {
   int64_t bkey, ckey;     // cell indices held, -1: none
-  float4 b0;              // depth corners
+  float4 b0;              // depth's bilinear coefficients
   float bx, by;           // dh/dx, dh/dy
-  float4 c0, c1, c2;      // u corners, v corners, gradients
+  float4 c0, c1, c2;      // u's and v's coefficients, the current's gradients
 };
 
 struct RayLane {
