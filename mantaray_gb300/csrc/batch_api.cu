@@ -256,6 +256,20 @@ cudaError_t enqueue(const mr_batch *b, mr::BatchArgs a, const mr_batch_config *c
 
 }  // namespace
 
+namespace mr {
+
+int batch_fill_args(mr_batch *b, size_t n, size_t n_stride, const uint8_t *ray_scenario,
+                    const double *x0, const double *y0, const double *kx0, const double *ky0,
+                    double t0, double dt, int64_t max_steps, int64_t decimation,
+                    size_t save_cap, float *saved, double *end_state, int32_t *n_steps,
+                    int32_t *n_saved, uint8_t *status, const mr_batch_config *cfg,
+                    BatchArgs *a) {
+  return fill_args(b, n, n_stride, ray_scenario, x0, y0, kx0, ky0, t0, dt, max_steps,
+                   decimation, save_cap, saved, end_state, n_steps, n_saved, status, cfg, a);
+}
+
+}  // namespace mr
+
 extern "C" {
 
 int mr_batch_default_config(mr_batch_config *cfg) {

@@ -39,3 +39,22 @@ inline int all_same_grid(const mr_batch *b) {
     if (!sc.same_grid) return 0;
   return 1;
 }
+
+struct mr_batch_config;
+
+namespace mr {
+
+// Checks the arguments of a batched call for n rays over buffers of n_stride
+// rays and fills the kernel's arguments (batch_api.cu).  Outputs may be
+// device memory or page-locked host memory (taken through its device
+// mapping); anything else fails with MR_ERR_INVALID_ARGUMENT before any work
+// is queued.  a->scen and a->queue are the batch's own device table and
+// work-queue head.  Allocates nothing.
+int batch_fill_args(mr_batch *b, size_t n, size_t n_stride, const uint8_t *ray_scenario,
+                    const double *x0, const double *y0, const double *kx0, const double *ky0,
+                    double t0, double dt, int64_t max_steps, int64_t decimation,
+                    size_t save_cap, float *saved, double *end_state, int32_t *n_steps,
+                    int32_t *n_saved, uint8_t *status, const mr_batch_config *cfg,
+                    BatchArgs *a);
+
+}  // namespace mr

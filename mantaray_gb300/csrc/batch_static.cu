@@ -77,65 +77,44 @@ extern "C" int mr_batch_trace_device_static(
                 "%d scenarios exceed the static scratch of mr_batch_trace_device_static "
                 "(at most %d scenarios); use mr_batch_trace_device",
                 b->n_scenarios, kStaticMaxScenarios);
-  if (!cfg) return fail(MR_ERR_INVALID_ARGUMENT, "null config");
-  if (cfg->block < 32 || cfg->block > 256 || cfg->block % 32 || cfg->blocks_per_sm < 1 ||
-      cfg->blocks_per_sm > 32 || (cfg->rays_per_lane != 1 && cfg->rays_per_lane != 2) ||
-      cfg->rebase_interval < 1)
-    return fail(MR_ERR_INVALID_ARGUMENT, "bad launch configuration");
-  if (cfg->order != 0)
+  if (cfg && cfg->order != 0)
     return fail(MR_ERR_INVALID_ARGUMENT,
                 "ray ordering needs scratch memory; use mr_batch_trace_device");
-  if (n > 0 && (!x0 || !y0 || !kx0 || !ky0 || !end_state || !n_steps || !n_saved || !status))
-    return fail(MR_ERR_INVALID_ARGUMENT, "null array argument");
-  if (decimation < 0 || max_steps < 0 || max_steps >= INT32_MAX)
-    return fail(MR_ERR_INVALID_ARGUMENT, "bad max_steps or decimation");
-  if (decimation > 0 && (!saved || static_cast<int64_t>(save_cap) < max_steps / decimation + 1))
-    return fail(MR_ERR_CAPACITY, "saved buffer too small for max_steps / decimation + 1 rows");
-  if (!(dt > 0.0) || !isfinite(t0)) return fail(MR_ERR_INVALID_ARGUMENT, "dt must be > 0");
+  // The same checks as mr_batch_trace_device, with the same messages:
+  // outputs must be device memory or page-locked host memory (written
+  // through its device mapping); pageable host memory is refused here,
+  // before anything is queued.
+  mr::BatchArgs a{};
+  int rc = mr::batch_fill_args(b, n, n, ray_scenario, x0, y0, kx0, ky0, t0, dt, max_steps,
+                               decimation, save_cap, saved, end_state, n_steps, n_saved, status,
+                               cfg, &a);
+  if (rc) return rc;
   if (n == 0) return MR_OK;
 
   DeviceGuard g(b->device);
   if (!g.ok()) return fail(MR_ERR_CUDA, "cannot select the batch's device");
   unsigned char *scratch = nullptr;
-  int rc = scratch_address(b->device, &scratch);
+  rc = scratch_address(b->device, &scratch);
   if (rc) return rc;
   unsigned long long *queue = reinterpret_cast<unsigned long long *>(scratch);
   mr::ScenarioDev *table = reinterpret_cast<mr::ScenarioDev *>(scratch + kQueueBytes);
-
-  mr::BatchArgs a{};
   a.scen = table;
-  a.scen0 = b->host_scen[0];
-  a.all_same_grid = all_same_grid(b);
-  a.n_scenarios = b->n_scenarios;
-  a.ray_scenario = ray_scenario;
-  a.n = static_cast<int64_t>(n);
-  a.x0 = x0; a.y0 = y0; a.kx0 = kx0; a.ky0 = ky0;
-  a.t0 = t0;
-  a.dt = dt;
-  a.dt_f = static_cast<float>(dt);
-  a.half_f = 0.5f * a.dt_f;
-  a.sixth_f = a.dt_f * (1.0f / 6.0f);
-  a.max_steps = max_steps;
-  a.decimation = decimation;
-  a.save_cap = static_cast<int64_t>(save_cap);
-  a.n_stride = static_cast<int64_t>(n);
-  a.rebase_interval = cfg->rebase_interval;
-  a.saved = saved;
-  a.end_state = end_state;
-  a.n_steps = n_steps;
-  a.n_saved = n_saved;
-  a.status = status;
   a.queue = queue;
 
   // The scratch keeps the previous call's contents: the queue head must start
-  // at zero, and the scenario table is rewritten for this batch.
+  // at zero, and the scenario table is rewritten for this batch from the
+  // batch's own device copy (a device-to-device copy: no host staging).  The
+  // single-scenario builds take their scenario from the kernel's parameters
+  // and never read the table, so one scenario needs no copy.
   cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : cudaStreamPerThread;
-  cudaError_t e = cudaMemcpyAsync(table, b->host_scen.data(),
-                                  b->host_scen.size() * sizeof(mr::ScenarioDev),
-                                  cudaMemcpyHostToDevice, s);
+  cudaError_t e = cudaSuccess;
+  if (b->n_scenarios > 1)
+    e = cudaMemcpyAsync(table, b->scen, static_cast<size_t>(b->n_scenarios) * sizeof(mr::ScenarioDev),
+                        cudaMemcpyDeviceToDevice, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(queue, 0, sizeof(unsigned long long), s);
-  if (e == cudaSuccess && decimation > 0)
-    e = cudaMemsetAsync(saved, 0xFF, sizeof(float) * 5 * save_cap * n, s);
+  // rows a ray does not reach: the same NaN as mr_batch_trace_device writes
+  if (e == cudaSuccess && decimation > 0 && save_cap > 0)
+    e = mr::launch_fill_nan(a.saved, 5 * static_cast<int64_t>(save_cap) * a.n_stride, s);
   if (e == cudaSuccess)
     e = mr::launch_rk4_f32(a, cfg->block, cfg->blocks_per_sm, cfg->rays_per_lane, s);
   if (e != cudaSuccess) return cuda_fail(e, "rk4_f32 launch (static scratch)");
