@@ -60,6 +60,14 @@ ALG_FP32_FLOP_PER_RAY_STEP = 710.0
 FP64_FLOP_PER_RAY_STEP = {"libm": 1401.4, "identity": 343.6}
 # FP64-pipe instructions per ray-step (sm__inst_executed_pipe_fp64 x 32, same captures)
 FP64_PIPE_INST_PER_RAY_STEP = {"libm": 945.2, "identity": 283.6}
+# DRAM bytes (read + written) per ray-step of the plain kernel on the seamount
+# workload, from an ncu capture whose stored trajectory rows dwarf L2; None
+# until measured.
+K1_DRAM_BYTES_PER_RAY_STEP = None
+K1_DRAM_NOTE = ""
+# The same for the batched kernel on the shelf-slope field.
+K2_SHELF_DRAM_BYTES_PER_RAY_STEP = None
+K2_SHELF_DRAM_NOTE = ""
 
 
 def parse():
@@ -92,6 +100,25 @@ def parse():
     p.add_argument("--launch", default=None,
                    help="batched form: fixed launch shape 'block,blocks_per_sm,rays_per_lane,"
                         "order' instead of the autotuner's")
+    # the target measurements reported beside the plain form's line
+    p.add_argument("--no-north-star", action="store_true",
+                   help="plain form: skip the shelf-slope batched-vs-plain and adjoint-vs-"
+                        "forward measurements reported in the line's north_star object")
+    p.add_argument("--ns-rays", type=int, default=16777216,
+                   help="shelf-slope: nominal rays per call (each call traces 0.5-1.5x)")
+    p.add_argument("--ns-grid", type=int, default=8192, help="shelf-slope: grid points per axis")
+    p.add_argument("--ns-steps", type=int, default=50000, help="shelf-slope: step horizon")
+    p.add_argument("--ns-calls", type=int, default=6,
+                   help="shelf-slope: timed graph-replayed calls")
+    p.add_argument("--ns-warmup", type=int, default=2, help="shelf-slope: untimed calls")
+    p.add_argument("--ns-plain-rays", type=int, default=262144,
+                   help="shelf-slope: rays of the plain FP64 form's rate measurement")
+    p.add_argument("--ns-plain-chunk", type=int, default=2500,
+                   help="shelf-slope: steps per plain FP64 launch (memory of full trajectories)")
+    p.add_argument("--ns-error-rays", type=int, default=4096,
+                   help="shelf-slope: rays of the endpoint-error comparison")
+    p.add_argument("--ns-adjoint-calls", type=int, default=2,
+                   help="differentiation case: timed forward and gradient calls per precision")
     return p.parse_args()
 
 
@@ -409,15 +436,28 @@ def gb300_arm(args, rank: int, world: int, local_rank: int):
                        "frac": hbm_achieved / hbm_peak,
                        "bytes_per_ray_step": GRID_BYTES_PER_RAY_STEP + OUT_BYTES_PER_ROW,
                        "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"}
-    # DRAM bytes of one full launch, scaled from the ncu capture of 65,536 rays
-    # x 100 steps (217.03 MB) by ray-steps (profiles/rk4_f64_seamount_65536rays_100steps.md)
-    if args.workload == "seamount":
-        roofline["traffic"] = 217.03e6 * ray_steps / (65536 * 100)
-        roofline["traffic_note"] = "scaled from a 65,536-ray x 100-step ncu capture by ray-steps"
+    # DRAM bytes of one launch: the algorithmic floor (the trajectory rows the
+    # launch must store, NaN padding included) and the ncu count of a capture
+    # whose stored rows dwarf L2, scaled by ray-steps
+    must_store = 5 * 8 * rows * n + n * 5
+    roofline["traffic_floor"] = must_store
+    if args.workload == "seamount" and K1_DRAM_BYTES_PER_RAY_STEP is not None:
+        roofline["traffic"] = K1_DRAM_BYTES_PER_RAY_STEP * ray_steps
+        roofline["traffic_note"] = K1_DRAM_NOTE
     else:
         roofline["traffic"] = None
+        roofline["traffic_note"] = "no ncu capture of this workload"
+    if args.workload != "seamount":
         roofline["executed_note"] = "executed counts from ncu on the seamount workload"
     roofline["kernel_ms"] = 1e3 * kernel_s
+
+    # free the headline's buffers before the target measurements
+    del traj, n_rows, status, ins
+    torch.cuda.empty_cache()
+    north = None
+    if not args.no_north_star and world == 1:
+        north = {"batched_fp32": north_star_batched(args, dev, stream, flush),
+                 "adjoint": north_star_adjoint(args, dev, stream)}
 
     cpu = None
     if not args.no_cpu_baseline:
@@ -436,9 +476,299 @@ def gb300_arm(args, rank: int, world: int, local_rank: int):
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
         "clocks": clock,
     }
+    if north is not None:
+        line["north_star"] = north
+    elif not args.no_north_star:
+        line["north_star"] = {"skipped": f"{world} ranks: measured on one GPU only"}
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def plain_rate(b, c, rays, t0, dt, steps, chunk, dev, stream):
+    """The plain FP64 form (K1, one mr_trace_device launch per chunk of
+    `chunk` steps, full trajectories) over the whole step horizon of these
+    rays: a ray still running at the end of a chunk continues from its last
+    state in the next one (bit-identical to one launch: dt is a power of two,
+    so every chunk's start time is exact), ended rays are dropped between
+    chunks.  Only the launches are timed (CUDA events).  Returns
+    (ray-steps, seconds, launches)."""
+    import torch
+
+    import mantaray_gb300 as mr
+
+    n = int(rays[0].numel())
+    buf = torch.empty(5 * (chunk + 1) * n, dtype=torch.float64, device=dev)
+    nr = torch.empty(n, dtype=torch.int32, device=dev)
+    st = torch.empty(n, dtype=torch.uint8, device=dev)
+    cur = [r.contiguous() for r in rays]
+    t, left, ray_steps, seconds, launches = t0, steps, 0, 0.0, 0
+    while left > 0 and cur[0].numel() > 0:
+        k, m = min(chunk, left), int(cur[0].numel())
+        traj = buf[: 5 * (k + 1) * m].view(5, k + 1, m)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        mr.trace_device(b, c, *cur, t, t + k * dt, dt, traj, nr[:m], st[:m], math="identity",
+                        stream=stream)
+        e1.record(stream)
+        e1.synchronize()
+        seconds += e0.elapsed_time(e1) / 1e3
+        launches += 1
+        ray_steps += int((nr[:m].to(torch.int64) - 1).sum().item())
+        alive = st[:m] == 0  # MR_RAY_COMPLETE: every step of the chunk taken
+        cur = [traj[q, k][alive].contiguous() for q in range(1, 5)]
+        t += k * dt
+        left -= k
+    del buf
+    return ray_steps, seconds, launches
+
+
+def fp64_trajectories(b, c, rays, t0, dt, steps, dev, stream):
+    """Full plain FP64 trajectories (traj[5][steps + 1][n], rows) of these
+    rays, on the device."""
+    import torch
+
+    import mantaray_gb300 as mr
+
+    n = int(rays[0].numel())
+    traj = torch.empty((5, steps + 1, n), dtype=torch.float64, device=dev)
+    nr = torch.empty(n, dtype=torch.int32, device=dev)
+    st = torch.empty(n, dtype=torch.uint8, device=dev)
+    mr.trace_device(b, c, *rays, t0, t0 + steps * dt, dt, traj, nr, st, math="identity",
+                    stream=stream)
+    torch.cuda.synchronize()
+    return traj, nr
+
+
+def chunked_endpoint_errors(end, n_steps, traj, nr, per=512):
+    """batch.endpoint_errors of end states against device trajectories,
+    `per` rays at a time (small host copies).  Returns (relative position
+    errors, direction errors, rays compared)."""
+    from mantaray_gb300.batch import endpoint_errors
+
+    n = int(nr.numel())
+    rel, dth, compared = [], [], 0
+    for s in range(0, n, per):
+        e = slice(s, min(n, s + per))
+        er = endpoint_errors(end[:, e], n_steps[e], traj[:, :, e].cpu().numpy(),
+                             nr[e].cpu().numpy())
+        rel.append(er["rel_position"])
+        dth.append(er["direction"])
+        compared += er["compared"]
+    return np.concatenate(rel), np.concatenate(dth), compared
+
+
+def last_finite_states(traj, nr):
+    """Each ray's last finite row of device trajectories: (states [5][n], row)."""
+    import torch
+
+    n = int(nr.numel())
+    last = (nr.to(torch.int64) - 1).clamp(min=0)
+    idx = torch.arange(n, device=traj.device)
+    fin = torch.isfinite(traj[1:, last, idx]).all(dim=0)
+    last = torch.where(fin, last, (last - 1).clamp(min=0))
+    return traj[:, last, idx].cpu().numpy(), last.cpu().numpy()
+
+
+def north_star_batched(args, dev, stream, flush) -> dict:
+    """The large single-scenario throughput case: rays entering an 8,192^2
+    shelf-slope field at 50 m (h, u, v and their cell gradients as FP32 cell
+    records: 5.4 GB, far above L2) for up to 50,000 steps of 2 s, in
+    graph-replayed calls of the autotuned batched FP32 form whose ray counts
+    vary +-50% about 16,777,216 (seeded).  Beside it: the plain FP64 form's
+    rate on a subset of the same rays over the same horizon, and the batched
+    end states' error against plain FP64 trajectories of the same rays."""
+    import torch
+
+    import mantaray_gb300 as mr
+    from mantaray_gb300 import workloads as W
+    from mantaray_gb300.batch import BatchTracer
+
+    nominal = args.ns_rays
+    cap = nominal * 3 // 2
+    t_gen = time.perf_counter()
+    fields, rays = W.shelf_slope(n=args.ns_grid, n_rays=cap, steps=args.ns_steps)
+    t_gen = time.perf_counter() - t_gen
+    b = mr.Bathymetry.grid(fields[0], fields[1], fields[2])
+    c = mr.Current.grid(fields[3], fields[4], fields[5], fields[6])
+    del fields
+    tracer = BatchTracer([(b, c)])
+    ins = [torch.from_numpy(rays[k]).to(dev) for k in ("x0", "y0", "kx0", "ky0")]
+    steps, dt, t0 = rays["steps"], rays["dt"], rays["t0"]
+    name = (f"shelf_slope_{nominal}rays_pm50pct_{args.ns_grid}x{args.ns_grid}_dt2_"
+            f"{steps}steps_graph_replay")
+    probe = min(cap, 1 << 20)
+    cfg = tracer.autotune(*[t[:probe] for t in ins], dt, min(steps, 1000), t0=t0,
+                          cache_key=f"{torch.cuda.get_device_name(dev)}:{name}:{probe}")
+    g = tracer.graph(*ins, dt, steps, t0=t0, config=cfg)
+    out = g.out
+    counts = np.random.default_rng(4004).integers(nominal // 2, cap + 1,
+                                                  args.ns_warmup + args.ns_calls)
+    for i in range(args.ns_warmup):
+        g.launch(int(counts[i]), stream=stream)
+    torch.cuda.synchronize()
+    times, done = [], 0
+    with ClockSampler(dev.index or 0) as clocks:
+        for i in range(args.ns_calls):
+            cnt = int(counts[args.ns_warmup + i])
+            flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            g.launch(cnt, stream=stream)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+            done += int(out.n_steps[:cnt].to(torch.int64).sum().item())
+    clock = clocks.summary()
+    value = done / sum(times)
+    timed_counts = counts[args.ns_warmup:]
+
+    # endpoint errors against plain FP64 trajectories: rays every call traces
+    n_err = min(args.ns_error_rays, nominal // 2)
+    eidx = torch.from_numpy(np.linspace(0, nominal // 2 - 1, n_err).astype(np.int64)).to(dev)
+    end_b = out.end_state[:, eidx].cpu().numpy()
+    nst_b = out.n_steps[eidx].cpu().numpy()
+    stat_b = out.status[eidx].cpu().numpy()
+    erays = [t[eidx] for t in ins]
+    traj, nr = fp64_trajectories(b, c, erays, t0, dt, steps, dev, stream)
+    rel, dth, compared = chunked_endpoint_errors(end_b, nst_b, traj, nr)
+    # the FP64 model's own sensitivity: the same rays started 1 cm further in x
+    traj_p, nr_p = fp64_trajectories(b, c, [erays[0] + 0.01] + erays[1:], t0, dt, steps, dev,
+                                     stream)
+    end_p, last_p = last_finite_states(traj_p, nr_p)
+    del traj_p
+    sens, _, _ = chunked_endpoint_errors(end_p, last_p, traj, nr)
+    del traj
+
+    # the plain FP64 form's rate on a subset of the same rays, same horizon
+    n_plain = min(args.ns_plain_rays, nominal)
+    pidx = torch.from_numpy(np.linspace(0, cap - 1, n_plain).astype(np.int64)).to(dev)
+    plain_steps, plain_s, plain_launches = plain_rate(
+        b, c, [t[pidx] for t in ins], t0, dt, steps, args.ns_plain_chunk, dev, stream)
+    plain = plain_steps / plain_s
+
+    L = mr._native.load()
+    import ctypes
+
+    fp32_peak = ctypes.c_double()
+    mr._native.check(L.mr_measure_fma_peak(0, ctypes.byref(fp32_peak)))
+    ach = value * ALG_FP32_FLOP_PER_RAY_STEP / 1e12
+    roof = {"bound": "fp32", "achieved": ach, "peak": fp32_peak.value, "unit": "TFLOP/s",
+            "frac": ach / fp32_peak.value,
+            "peak_source": "measured: FP32 FMA-chain kernel on this GPU, this run",
+            "flop_per_ray_step": ALG_FP32_FLOP_PER_RAY_STEP,
+            "executed_flop_per_ray_step": FP32_FLOP_PER_RAY_STEP,
+            "executed_frac": value * FP32_FLOP_PER_RAY_STEP / 1e12 / fp32_peak.value}
+    if K2_SHELF_DRAM_BYTES_PER_RAY_STEP is not None:
+        roof["traffic"] = K2_SHELF_DRAM_BYTES_PER_RAY_STEP * done / args.ns_calls
+        roof["traffic_note"] = K2_SHELF_DRAM_NOTE
+    roof["traffic_floor"] = float(np.mean(timed_counts)) * (4 * 8 + 5 * 8 + 4 + 4 + 1)
+    status = np.bincount(stat_b, minlength=4)
+    return {
+        "workload": name, "metric": METRIC, "value": value, "unit": METRIC, "dtype": "f32",
+        "calls": args.ns_calls, "warmup_calls": args.ns_warmup,
+        "ms_per_call": 1e3 * sum(times) / args.ns_calls,
+        "rays_per_call": {"min": int(timed_counts.min()), "max": int(timed_counts.max()),
+                          "mean": float(timed_counts.mean()), "capacity": cap},
+        "ray_steps_per_call": done / args.ns_calls, "max_steps": steps, "dt": dt,
+        "graph_replay": True, "launch": cfg.as_dict(), "autotuned": True,
+        "field": f"{args.ns_grid}^2 f32 cell records (h, u, v, gradients), generated in "
+                 f"{t_gen:.0f} s on the host",
+        "l2": "512 MB buffer written between timed calls; cell records 5.4 GB > L2",
+        "plain_fp64_same_rays": {"value": plain, "unit": METRIC, "rays": n_plain,
+                                 "ray_steps": plain_steps, "launches": plain_launches,
+                                 "chunk_steps": args.ns_plain_chunk, "math": "identity",
+                                 "how": "mr_trace_device per chunk of steps over the whole "
+                                        "horizon, running rays continued, launches timed"},
+        "batched_over_plain": value / plain, "target_batched_over_plain": ">= 5",
+        "endpoint_error_vs_fp64": {
+            "rays": compared, "of": n_err,
+            "status_counts": {"complete": int(status[0]), "out_of_domain": int(status[1]),
+                              "dry": int(status[2]), "bad_wavenumber": int(status[3])},
+            "rel_position_p50": float(np.median(rel)),
+            "rel_position_p99": float(np.percentile(rel, 99)),
+            "rel_position_max": float(rel.max()),
+            "direction_p99_rad": float(np.percentile(dth, 99)),
+            "direction_max_rad": float(dth.max()), "target_rel_position": "<= 1e-3"},
+        "fp64_endpoint_change_for_1cm_start_shift": {
+            "rel_position_p50": float(np.median(sens)),
+            "rel_position_p99": float(np.percentile(sens, 99)),
+            "rel_position_max": float(sens.max())},
+        "roofline": roof, "clocks": clock,
+        "gpu_launches": args.ns_calls,
+    }
+
+
+def adjoint_times(precision, n_rays, steps, warmup, calls, dev, stream):
+    """Forward (with checkpoints) and forward + gradient times of the
+    differentiation case (262,144 rays x 3,000 steps on the 512^2 shelf-bump
+    field, checkpoints every 55 steps, endpoint (y, theta) misfit loss against
+    targets traced with the shoal raised 10%)."""
+    import torch
+
+    from mantaray_gb300.diff import endpoint_loss, grid, ray_endpoints
+    from mantaray_gb300.workloads import shelf_bump
+
+    w = shelf_bump(n_rays=n_rays, steps=steps)
+    tg = shelf_bump(n_rays=n_rays, steps=steps, bump_scale=1.1)
+    dtype = torch.float64 if precision == 64 else torch.float32
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev).to(dtype)  # noqa: E731
+    g = grid(512, 512, 0.0, 0.0, 200.0, 200.0)
+    rays = [t(a) for a in (w.x0, w.y0, w.kx0, w.ky0)]
+    D, U, V = t(w.depth), t(w.u), t(w.v)
+    every = 55
+    tgt, tst = ray_endpoints(*rays, t(tg.depth), U, V, g, g, 1.0, steps, every)
+    y_t, th_t = tgt[1], torch.atan2(tgt[3], tgt[2])
+
+    def forward_only():
+        with torch.no_grad():
+            return ray_endpoints(*rays, D, U, V, g, g, 1.0, steps, every)
+
+    def gradient():
+        depth = D.clone().requires_grad_(True)
+        u = U.clone().requires_grad_(True)
+        v = V.clone().requires_grad_(True)
+        r = [x.clone().requires_grad_(True) for x in rays]
+        end, status = ray_endpoints(*r, depth, u, v, g, g, 1.0, steps, every)
+        keep = (status == 0) & (tst == 0)
+        loss = endpoint_loss(end, torch.where(keep, status, torch.ones_like(status)), y_t, th_t)
+        loss.backward()
+        return loss
+
+    def timed(fn):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(calls):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1) / 1e3)
+        return sum(ts) / len(ts)
+
+    t_fwd = timed(forward_only)
+    t_grad = timed(gradient)
+    return w, t_fwd, t_grad
+
+
+def north_star_adjoint(args, dev, stream) -> dict:
+    """Gradient / forward time of the differentiation case, FP64 and FP32."""
+    res = {"workload": "shelf_bump_262144rays_512x512_dt1_3000steps_checkpoints55",
+           "calls": args.ns_adjoint_calls, "target_gradient_over_forward": "<= 5"}
+    with ClockSampler(dev.index or 0) as clocks:
+        for prec in (64, 32):
+            _, t_fwd, t_grad = adjoint_times(prec, 262144, 3000, 1, args.ns_adjoint_calls, dev,
+                                             stream)
+            res[f"fp{prec}"] = {"forward_ms": 1e3 * t_fwd, "gradient_ms": 1e3 * t_grad,
+                                "gradient_over_forward": t_grad / t_fwd}
+    res["clocks"] = clocks.summary()
+    return res
 
 
 def batched_arm(args, rank: int, world: int, local_rank: int):
@@ -762,58 +1092,15 @@ def adjoint_arm(args, rank: int, world: int, local_rank: int):
     import torch
 
     import mantaray_gb300 as mr
-    from mantaray_gb300.diff import endpoint_loss, grid, ray_endpoints
-    from mantaray_gb300.workloads import shelf_bump
 
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
     n_rays = args.rays if args.rays != 65536 else 262144
     steps = args.trace_steps if args.trace_steps != 4000 else 3000
-    w = shelf_bump(n_rays=n_rays, steps=steps)
-    tg = shelf_bump(n_rays=n_rays, steps=steps, bump_scale=1.1)
-    dtype = torch.float64 if args.precision == 64 else torch.float32
-    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev).to(dtype)  # noqa: E731
-    g = grid(512, 512, 0.0, 0.0, 200.0, 200.0)
-    rays = [t(a) for a in (w.x0, w.y0, w.kx0, w.ky0)]
-    D, U, V = t(w.depth), t(w.u), t(w.v)
-    every = 55
-    tgt, tst = ray_endpoints(*rays, t(tg.depth), U, V, g, g, 1.0, steps, every)
-    y_t, th_t = tgt[1], torch.atan2(tgt[3], tgt[2])
     stream = torch.cuda.current_stream(dev)
-
-    def forward_only():
-        with torch.no_grad():
-            return ray_endpoints(*rays, D, U, V, g, g, 1.0, steps, every)
-
-    def gradient():
-        depth = D.clone().requires_grad_(True)
-        u = U.clone().requires_grad_(True)
-        v = V.clone().requires_grad_(True)
-        r = [x.clone().requires_grad_(True) for x in rays]
-        end, status = ray_endpoints(*r, depth, u, v, g, g, 1.0, steps, every)
-        keep = (status == 0) & (tst == 0)
-        loss = endpoint_loss(end, torch.where(keep, status, torch.ones_like(status)), y_t, th_t)
-        loss.backward()
-        return loss
-
-    def timed(fn):
-        for _ in range(args.warmup):
-            fn()
-        torch.cuda.synchronize()
-        ts = []
-        for _ in range(args.steps):
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            fn()
-            e1.record(stream)
-            e1.synchronize()
-            ts.append(e0.elapsed_time(e1) / 1e3)
-        return sum(ts) / len(ts)
-
     with ClockSampler(local_rank) as clocks:
-        t_fwd = timed(forward_only)
-        t_grad = timed(gradient)
+        w, t_fwd, t_grad = adjoint_times(args.precision, n_rays, steps, args.warmup, args.steps,
+                                         dev, stream)
     clock = clocks.summary()
     # the plain FP64 drop-in kernel over the same rays and fields (f32-cast
     # lookups, as the reference), for scale
@@ -824,12 +1111,18 @@ def adjoint_arm(args, rank: int, world: int, local_rank: int):
     traj = torch.empty((5, steps + 1, sub), dtype=torch.float64, device=dev)
     nr = torch.empty(sub, dtype=torch.int32, device=dev)
     st = torch.empty(sub, dtype=torch.uint8, device=dev)
-
-    def plain():
+    times = []
+    for i in range(args.warmup + args.steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
         mr.trace_device(b, c, *pin, 0.0, float(steps), 1.0, traj, nr, st, math="identity",
                         stream=stream)
-
-    t_plain = timed(plain) * n_rays / sub
+        e1.record(stream)
+        e1.synchronize()
+        if i >= args.warmup:
+            times.append(e0.elapsed_time(e1) / 1e3)
+    t_plain = statistics.mean(times) * n_rays / sub
     ray_steps = n_rays * steps
     if rank != 0:
         return
@@ -840,7 +1133,7 @@ def adjoint_arm(args, rank: int, world: int, local_rank: int):
         "dtype": "f64" if args.precision == 64 else "f32", "data": "synthetic",
         "config": {"workload": w.name, "form": "differentiation: forward with checkpoints + "
                                                "discrete adjoint (mr_diff_*)",
-                   "rays": n_rays, "steps_per_ray": steps, "checkpoint_every": every,
+                   "rays": n_rays, "steps_per_ray": steps, "checkpoint_every": 55,
                    "gradient_ms": 1e3 * t_grad, "forward_ms": 1e3 * t_fwd,
                    "plain_fp64_forward_ms": 1e3 * t_plain,
                    "gradient_over_forward": t_grad / t_fwd,

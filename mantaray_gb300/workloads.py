@@ -194,7 +194,8 @@ def multi_source(n_sources: int = 1024, rays_per_source: int = 4096, n_scenarios
     return scenarios, rays
 
 
-def shelf_slope(n: int = 8192, n_rays: int = 16777216, steps: int = 50000, seed: int = 1004):
+def shelf_slope(n: int = 8192, n_rays: int = 16777216, steps: int = 50000, seed: int = 1004,
+                spacing: float = 50.0):
     """Large single-scenario case: 8,192 x 8,192 grid at 50 m.  Bathymetry: a
     continental shelf-slope profile along x (4,000 m deep at the entry edge,
     a tanh slope centred at 300 km, 15 km wide, up to a 60 m shelf) plus
@@ -203,13 +204,16 @@ def shelf_slope(n: int = 8192, n_rays: int = 16777216, steps: int = 50000, seed:
     meander amplitude 30 km, wavelength 150 km) plus 64 seeded Gaussian eddies
     (0.2-1.0 m/s, sigma 5-20 km).  Swell enters at x = 0 with y ~ U over the
     edge, directions ~ U(+-15 deg), periods ~ U[10, 16] s; dt = 2 s, up to
-    50,000 steps.  Returns (fields, rays) like multi_source (one scenario)."""
+    50,000 steps.  Returns (fields, rays) like multi_source (one scenario).
+    A smaller n at the same spacing is a corner of that domain; n = 1,024 at
+    a `spacing` of 400 m keeps the whole domain (slope, shelf, jet, eddies)
+    on a coarser grid."""
     rng = np.random.default_rng(seed)
-    x = np.arange(n, dtype=np.float64) * 50.0
+    x = np.arange(n, dtype=np.float64) * spacing
     profile = 60.0 + (4000.0 - 60.0) * 0.5 * (1.0 - np.tanh((x - 300000.0) / 15000.0))
     # random-phase k^-3 roughness (FFT synthesis on the grid)
-    kx = np.fft.fftfreq(n, d=50.0)
-    ky = np.fft.rfftfreq(n, d=50.0)
+    kx = np.fft.fftfreq(n, d=spacing)
+    ky = np.fft.rfftfreq(n, d=spacing)
     kk = np.hypot(kx[:, None], ky[None, :])
     amp = np.zeros_like(kk)
     nz = kk > 0
@@ -231,7 +235,9 @@ def shelf_slope(n: int = 8192, n_rays: int = 16777216, steps: int = 50000, seed:
     theta = rng.uniform(-np.deg2rad(15.0), np.deg2rad(15.0), n_rays)
     period = rng.uniform(10.0, 16.0, n_rays)
     x0 = np.zeros(n_rays)
-    kx0, ky0 = wavenumber_vector(period, np.full(n_rays, profile[0]), theta)
+    # |k0| at the launch depth h(0, y0): the grid's x = 0 column interpolated
+    # linearly in y (the bilinear at a zero x fraction), roughness included
+    kx0, ky0 = wavenumber_vector(period, np.interp(y0, x, depth[:, 0]), theta)
     fields = (x.astype(np.float32), x.astype(np.float32), depth, x, x, u, v)
     rays = {"x0": x0, "y0": y0, "kx0": kx0, "ky0": ky0, "scenario": None, "t0": 0.0, "dt": 2.0,
             "steps": steps}

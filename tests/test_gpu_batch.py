@@ -361,3 +361,104 @@ def test_edge_rays_get_their_status(mr):
     out = tracer.trace(*empty, 1.0, 10)
     torch.cuda.synchronize()
     assert out.n_steps.numel() == 0
+
+
+@pytest.mark.parametrize("size", ["fine_corner", "whole_domain"])
+def test_shelf_slope_against_oracle(mr, oracle, size):
+    # The large single-scenario case's generator at test size (as in the
+    # plain form's parity test): the batched FP32 end states against the
+    # oracle's trajectories of the same rays, and the same rays through a
+    # captured graph give the same bits as the direct call.
+    from mantaray_gb300.batch import BatchTracer, endpoint_errors
+    from mantaray_gb300.workloads import shelf_slope
+
+    kw = (dict(n=2048, n_rays=2048, steps=2000) if size == "fine_corner"
+          else dict(n=1024, spacing=400.0, n_rays=512, steps=20000))
+    f, r = shelf_slope(**kw)
+    b = mr.Bathymetry.grid(f[0], f[1], f[2])
+    c = mr.Current.grid(f[3], f[4], f[5], f[6])
+    tracer = BatchTracer([(b, c)])
+    ins = _dev(r["x0"], r["y0"], r["kx0"], r["ky0"])
+    res = tracer.trace(*ins, r["dt"], r["steps"], t0=r["t0"])
+    ob = oracle.Bathymetry.grid(f[0], f[1], f[2])
+    oc = oracle.Current.grid(f[3], f[4], f[5], f[6])
+    o = oracle.trace(ob, oc, r["x0"], r["y0"], r["kx0"], r["ky0"], r["t0"],
+                     r["t0"] + r["steps"] * r["dt"], r["dt"])
+    end, nst = res.end_state.cpu().numpy(), res.n_steps.cpu().numpy()
+    check_errors(endpoint_errors(end, nst, o[0], o[1]), size)
+    g = tracer.graph(*ins, r["dt"], r["steps"], t0=r["t0"])
+    g.launch()
+    np.testing.assert_array_equal(g.out.end_state.cpu().numpy(), end)
+    np.testing.assert_array_equal(g.out.n_steps.cpu().numpy(), nst)
+    g.close()
+
+
+def test_eight_scenarios_on_1024_grids(mr, oracle):
+    # The batching case's generator with its 8 scenarios at 1,024^2 (100 m;
+    # every current on its bathymetry's grid: the scenario-table build that
+    # takes one cell lookup for both fields), 64 point sources x 64 rays,
+    # 2,000 steps of 2 s, every 100th step stored.  Each ray against the
+    # oracle on its own scenario's fields, and bit for bit against the same
+    # rays traced through a one-scenario batch of that scenario.
+    from mantaray_gb300.batch import BatchTracer, endpoint_errors
+    from mantaray_gb300.workloads import multi_source
+
+    scen, rays = multi_source(n_sources=64, rays_per_source=64, n_scenarios=8, n=1024,
+                              steps=2000)
+    fields = [(mr.Bathymetry.grid(s[0], s[1], s[2]), mr.Current.grid(s[3], s[4], s[5], s[6]))
+              for s in scen]
+    tracer = BatchTracer(fields)
+    ins = _dev(rays["x0"], rays["y0"], rays["kx0"], rays["ky0"])
+    (sid,) = _dev(rays["scenario"])
+    res = tracer.trace(*ins, rays["dt"], 2000, decimation=100, scenario=sid)
+    end, nst = res.end_state.cpu().numpy(), res.n_steps.cpu().numpy()
+    saved = res.saved.cpu().numpy()
+    assert np.any(res.status.cpu().numpy() != 0)  # uneven lifetimes
+    for s in range(8):
+        m = rays["scenario"] == s
+        ob = oracle.Bathymetry.grid(*scen[s][:3])
+        oc = oracle.Current.grid(*scen[s][3:])
+        o = oracle.trace(ob, oc, *(rays[k][m] for k in ("x0", "y0", "kx0", "ky0")), 0.0,
+                         2000 * rays["dt"], rays["dt"])
+        check_errors(endpoint_errors(end[:, m], nst[m], o[0], o[1]), f"scenario {s}")
+        one = BatchTracer([fields[s]]).trace(*_dev(*(rays[k][m] for k in
+                                                     ("x0", "y0", "kx0", "ky0"))),
+                                             rays["dt"], 2000, decimation=100)
+        np.testing.assert_array_equal(one.end_state.cpu().numpy(), end[:, m])
+        np.testing.assert_array_equal(one.n_steps.cpu().numpy(), nst[m])
+        np.testing.assert_array_equal(one.saved.cpu().numpy().view(np.uint32),
+                                      saved[:, :, m].view(np.uint32))
+
+
+def test_autotuner_candidates_cache_and_results(mr, tmp_path, monkeypatch):
+    # The autotuner returns one of its candidates, records it under the key in
+    # memory and in $MANTARAY_TUNE_CACHE (read back by a fresh process's
+    # empty memory cache), and the shape it picks changes no result bit.
+    import json
+
+    from mantaray_gb300 import batch as B
+    from mantaray_gb300.workloads import seamount
+
+    w = seamount(n_rays=16384, steps=200)
+    tracer = B.BatchTracer([_fields(mr, w)])
+    ins = _dev(w.x0, w.y0, w.kx0, w.ky0)
+    path = tmp_path / "tune.json"
+    monkeypatch.setenv("MANTARAY_TUNE_CACHE", str(path))
+    monkeypatch.setattr(B, "_TUNE_CACHE", {})
+    cands = [B.make_config(64, 8, 1, 32, 0), B.make_config(128, 4, 2, 32, 1),
+             B.make_config(256, 2, 1, 32, 0)]
+    cfg = tracer.autotune(*ins, w.dt, 200, candidates=cands, cache_key="seamount-test")
+    assert cfg.as_dict() in [c.as_dict() for c in cands]
+    stored = json.loads(path.read_text())
+    assert stored["seamount-test"] == cfg.as_dict()
+    monkeypatch.setattr(B, "_TUNE_CACHE", {})
+    again = tracer.autotune(*ins, w.dt, 200, candidates=cands[:1], cache_key="seamount-test")
+    assert again.as_dict() == cfg.as_dict()  # from the file: no new timing
+    tuned = tracer.trace(*ins, w.dt, 200, decimation=20, config=cfg)
+    base = tracer.trace(*ins, w.dt, 200, decimation=20, config=B.default_config())
+    for a, b_ in zip((tuned.end_state, tuned.n_steps, tuned.status, tuned.saved),
+                     (base.end_state, base.n_steps, base.status, base.saved)):
+        x, y = a.cpu().numpy(), b_.cpu().numpy()
+        if x.dtype == np.float32:
+            x, y = x.view(np.uint32), y.view(np.uint32)
+        np.testing.assert_array_equal(x, y)

@@ -5,10 +5,11 @@ finite differences on seeded nodes (delta h = 1e-3 m), the FP32 adjoint
 against the FP64 one, and the torch.autograd.Function.
 
 Bars: TLM vs FD <= 1e-5 relative (99% of the rays whose finite differences
-converge); adjoint vs TLM <= 1e-10 relative; adjoint vs FD on nodes <= 1e-5
-relative (FP64).  The map is smooth only inside grid cells (the cell-constant
-gradients jump at cell edges), so finite differences are used only where two
-step sizes agree."""
+converge, and at least 70-90% of the rays converging); adjoint vs TLM <= 1e-10
+relative; adjoint vs FD <= 1e-5 relative (FP64) on every one of 64 seeded
+nodes that has a converging ray, at least 48 of them.  The map is smooth only
+inside grid cells (the cell-constant gradients jump at cell edges), so finite
+differences are used only where two step sizes agree."""
 
 import numpy as np
 import pytest
@@ -60,11 +61,24 @@ def test_forward_matches_oracle_model(oracle, case):
     assert float(np.max(np.abs(e[:, ok] - o_end[:, ok]) / scale)) <= 1e-9
 
 
+# Finite differences of the oracle model, central, at two step sizes h and
+# h/2.  The model is smooth only between cell edges (its cell-constant
+# gradients jump there, so a run whose ray stage crosses an edge that the
+# other run does not measures the jump: 1e-2 and above), and each end state
+# carries rounding that the ray's own sensitivity amplifies (~45x through
+# the shoal's caustics: ~5e-10 m on x).  Two step sizes that agree to
+# CONSISTENT tell a smooth neighbourhood from a jump; the derivative is then
+# the Richardson value fd(h/2) + (fd(h/2) - fd(h)) / 3, whose eps^2 error
+# cancels.
+CONSISTENT = 3e-6
+
+
+def _richardson(fd1, fd2):
+    return fd2 + (fd2 - fd1) / 3.0
+
+
 def _consistent(fd1, fd2, floor):
-    """Finite differences at two step sizes that agree: the map is smooth
-    between the +/- runs (no stage crossed a cell edge, where the
-    cell-constant gradients jump)."""
-    return np.abs(fd1 - fd2) <= 1e-6 * np.maximum(np.abs(fd2), floor)
+    return np.abs(fd1 - fd2) <= CONSISTENT * np.maximum(np.abs(fd2), floor)
 
 
 def test_tangent_matches_finite_differences(oracle, case):
@@ -79,14 +93,18 @@ def test_tangent_matches_finite_differences(oracle, case):
     blob = np.exp(-((X - 51200.0) ** 2 + (Y - 51200.0) ** 2) / (2 * 6000.0 ** 2))
     ds0 = np.stack([rng.normal(0, 1.0, n), rng.normal(0, 1.0, n), rng.normal(0, 1e-4, n),
                     rng.normal(0, 1e-4, n)])
-    cases = [("state", ds0, None, None), ("depth", np.zeros((4, n)), 50.0 * blob, None),
-             ("u", np.zeros((4, n)), None, 0.1 * blob)]
+    # (name, state direction, depth direction, u direction, step sizes, least
+    # share of rays whose differences converge; measured on this case: 83%,
+    # 98% and 79%).  The current's direction takes larger steps: its end-state
+    # changes are small against the rounding above.
+    cases = [("state", ds0, None, None, (1e-4, 5e-5), 0.75),
+             ("depth", np.zeros((4, n)), 50.0 * blob, None, (1e-4, 5e-5), 0.90),
+             ("u", np.zeros((4, n)), None, 0.1 * blob, (1e-3, 5e-4), 0.70)]
     dev = case["depth"].device
-    # floors: below them a finite difference is rounding (end x, y ~ 5e4 m
-    # carry ~1e-11 m of rounding, / 2 eps = 5e-8 m; end kx, ky ~ 0.03 carry
-    # ~4e-18, / 2 eps = 2e-14)
-    floors = (1e-1, 1e-1, 1e-7, 1e-7)
-    for name, dst, dd, du in cases:
+    # floors: the rounding of a difference (5e-10 m / 2 h on x and y,
+    # 1.5e-16 / 2 h on kx and ky) stays below CONSISTENT times them
+    floors = (1.0, 1.0, 1e-6, 1e-6)
+    for name, dst, dd, du, steps_h, least in cases:
         _, d_end, st = tangent(*case["rays"], case["depth"], case["u"], case["v"], case["g"],
                                case["g"], case["dt"], case["steps"],
                                dstate0=torch.from_numpy(dst).to(dev),
@@ -95,7 +113,7 @@ def test_tangent_matches_finite_differences(oracle, case):
         d_end = d_end.cpu().numpy()
         ok = st.cpu().numpy() == 0
         fds = []
-        for eps in (1e-4, 5e-5):
+        for eps in steps_h:
             rp = [a + eps * dst[q] for q, a in enumerate((w.x0, w.y0, w.kx0, w.ky0))]
             rm = [a - eps * dst[q] for q, a in enumerate((w.x0, w.y0, w.kx0, w.ky0))]
             ep, sp = _oracle_end(oracle, case, depth=None if dd is None else w.depth + eps * dd,
@@ -107,12 +125,13 @@ def test_tangent_matches_finite_differences(oracle, case):
         clean = ok.copy()
         for q in range(4):
             clean &= _consistent(fds[0][q], fds[1][q], floors[q])
-        assert clean.sum() >= 0.4 * n, (name, int(clean.sum()))
+        assert clean.sum() >= least * n, (name, f"{int(clean.sum())} of {n} rays converge")
+        fd = _richardson(fds[0], fds[1])
         for q in range(4):
-            a, b = d_end[q, clean], fds[1][q, clean]
+            a, b = d_end[q, clean], fd[q, clean]
             rel = np.abs(a - b) / np.maximum(np.abs(b), floors[q])
-            # <= 1e-5 for 99% of the clean rays; a ray that grazes a caustic
-            # of the shoal can sit a little above it (seen: 1.7e-5)
+            # <= 1e-5 for 99% of the converging rays; a ray that grazes a
+            # caustic of the shoal can sit a little above it
             assert float(np.percentile(rel, 99)) <= 1e-5, (name, q, float(np.percentile(rel, 99)))
             assert float(rel.max()) <= 1e-4, (name, q, float(rel.max()))
 
@@ -151,10 +170,19 @@ def test_adjoint_dot_product(case):
 
 
 def test_adjoint_node_gradients_against_finite_differences(oracle, case):
-    # the differentiation case's loss against targets traced over the same
-    # field with the shoal raised 10%; FD on 64 seeded depth nodes with
-    # dh = 1e-3 m (and 5e-4 m to tell a smooth neighbourhood from one where a
-    # ray stage crosses a cell edge between the +/- runs)
+    # The differentiation case's loss against targets traced over the same
+    # field with the shoal raised 10%, on 64 seeded depth nodes that the
+    # rays' cells visit (nodes whose gradient is at least 1e-3 of the
+    # largest: in deep water depth does not enter the equations to double
+    # precision).  Central differences with dh = 1e-3 m (and 5e-4 m), taken
+    # ray by ray: the loss difference of each ray is formed from its own end
+    # states, so rays the node does not touch contribute exactly zero.  A ray
+    # whose two differences disagree crossed a cell edge in one run and not
+    # the other (a jump, not a derivative); the node's finite difference is
+    # then the sum over the converging rays, and the adjoint is run for the
+    # loss of exactly those rays (the adjoint is linear in the loss's terms).
+    # Every node with a converging ray is checked at 1e-5; at least 48 of the
+    # 64 must have one.
     import torch
 
     from mantaray_gb300.diff import endpoint_loss, ray_endpoints
@@ -163,38 +191,58 @@ def test_adjoint_node_gradients_against_finite_differences(oracle, case):
     tgt, tst = ray_endpoints(*case["rays"], case["t_depth"], case["u"], case["v"], case["g"],
                              case["g"], case["dt"], case["steps"])
     y_t, th_t = tgt[1].detach(), torch.atan2(tgt[3], tgt[2]).detach()
-    depth = case["depth"].clone().requires_grad_(True)
-    end, status = ray_endpoints(*case["rays"], depth, case["u"], case["v"], case["g"], case["g"],
-                                case["dt"], case["steps"])
-    keep = (status == 0) & (tst == 0)
-    loss = endpoint_loss(end, torch.where(keep, status, torch.ones_like(status)), y_t, th_t)
-    loss.backward()
-    grad = depth.grad.cpu().numpy()
-    keep_np = keep.cpu().numpy()
-    y_np, th_np = y_t.cpu().numpy(), th_t.cpu().numpy()
-    assert float(loss) > 1.0  # the rays do cross the shoal
 
-    def oracle_loss(dep):
-        e, s = _oracle_end(oracle, case, depth=dep)
-        m = keep_np & (s == 0)
-        th = np.arctan2(e[3], e[2])
-        return float(np.sum((e[1, m] - y_np[m]) ** 2 + (th[m] - th_np[m]) ** 2))
+    def adjoint(mask):
+        depth = case["depth"].clone().requires_grad_(True)
+        end, status = ray_endpoints(*case["rays"], depth, case["u"], case["v"], case["g"],
+                                    case["g"], case["dt"], case["steps"])
+        keep = (status == 0) & (tst == 0) & mask
+        loss = endpoint_loss(end, torch.where(keep, status, torch.ones_like(status)), y_t, th_t)
+        loss.backward()
+        return depth.grad.cpu().numpy(), keep.cpu().numpy(), float(loss)
+
+    dev = case["depth"].device
+    grad, keep_np, loss = adjoint(torch.ones(w.n, dtype=torch.bool, device=dev))
+    assert loss > 1.0  # the rays do cross the shoal
+    y_np, th_np = y_t.cpu().numpy(), th_t.cpu().numpy()
+
+    def ray_loss_differences(dp, dm):
+        ep, sp = _oracle_end(oracle, case, depth=dp)
+        em, sm = _oracle_end(oracle, case, depth=dm)
+        m = keep_np & (sp == 0) & (sm == 0)
+        thp, thm = np.arctan2(ep[3], ep[2]), np.arctan2(em[3], em[2])
+        d = ((ep[1] - em[1]) * (ep[1] + em[1] - 2.0 * y_np) +
+             (thp - thm) * (thp + thm - 2.0 * th_np))
+        return np.where(m, d, 0.0), m
 
     rng = np.random.default_rng(51)
     cand = np.argwhere(np.abs(grad) > 1e-3 * np.abs(grad).max())
     nodes = cand[rng.choice(len(cand), 64, replace=False)]
-    rel, clean = [], 0
+    report, worst = [], 0.0
     for j, i in nodes:
-        fd = []
+        fd, both = [], keep_np.copy()
         for d in (1e-3, 5e-4):
             dp = w.depth.copy(); dp[j, i] += d
             dm = w.depth.copy(); dm[j, i] -= d
-            fd.append((oracle_loss(dp) - oracle_loss(dm)) / (2 * d))
-        if abs(fd[0] - fd[1]) <= 1e-6 * abs(fd[1]):
-            clean += 1
-            rel.append(abs(grad[j, i] - fd[0]) / abs(fd[0]))
-    assert clean >= 16, clean
-    assert max(rel) <= 1e-5, rel
+            diff, m = ray_loss_differences(dp, dm)
+            both &= m
+            fd.append(diff / (2 * d))
+        touched = both & ((fd[0] != 0) | (fd[1] != 0))
+        scale = np.abs(fd[1][touched]).sum()
+        conv = touched & (np.abs(fd[0] - fd[1]) <= CONSISTENT * np.maximum(np.abs(fd[1]),
+                                                                          1e-9 * scale))
+        report.append((int(j), int(i), int(touched.sum()), int(conv.sum())))
+        if not conv.any():
+            continue
+        fd_node = float(np.sum(_richardson(fd[0], fd[1])[conv]))
+        g, _, _ = adjoint(torch.from_numpy(conv).to(dev))
+        rel = abs(g[j, i] - fd_node) / abs(fd_node)
+        assert rel <= 1e-5, (int(j), int(i), float(g[j, i]), fd_node, rel)
+        worst = max(worst, rel)
+    checked = sum(1 for r in report if r[3] > 0)
+    print(f"node gradients: {checked}/64 nodes checked (worst {worst:.2e}); "
+          f"(j, i, rays touched, rays converging): {report}")
+    assert checked >= 48, f"{checked}/64 nodes checked: {report}"
 
 
 def test_fp32_adjoint_follows_fp64(case):

@@ -390,3 +390,24 @@ def test_vortex_field_and_shelf_bump(mr, oracle):
     check(*r)
     w = shelf_bump(n_rays=256, steps=2000)
     check(*_workload_both(mr, oracle, w))
+
+
+@pytest.mark.parametrize("size", ["fine_corner", "whole_domain"])
+def test_shelf_slope_fields_every_row(mr, oracle, size):
+    # The large single-scenario case's generator (shelf-slope profile, k^-3
+    # roughness at 50 m rms, meandering jet and 64 eddies; |k0| at the launch
+    # depth), every row of every ray against the oracle: at its own 50 m
+    # spacing on a 2,048^2 corner of the domain (the roughness at full
+    # resolution; 2,048 rays x 2,000 steps), and over its whole 409.6 km
+    # domain on a 1,024^2 grid at 400 m, where the rays cross the slope onto
+    # the 60 m shelf (512 rays x 20,000 steps; about half end at the shore
+    # or a side edge).
+    from mantaray_gb300.workloads import shelf_slope
+
+    kw = (dict(n=2048, n_rays=2048, steps=2000) if size == "fine_corner"
+          else dict(n=1024, spacing=400.0, n_rays=512, steps=20000))
+    f, r = shelf_slope(**kw)
+    res = both(mr, oracle, ("grid",) + tuple(f[:3]), ("grid",) + tuple(f[3:]), r["x0"], r["y0"],
+               r["kx0"], r["ky0"], r["t0"], r["t0"] + r["steps"] * r["dt"], r["dt"])
+    check(*res)
+    assert np.any(res[2] != 0) or size == "fine_corner"
