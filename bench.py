@@ -61,10 +61,13 @@ FP64_FLOP_PER_RAY_STEP = {"libm": 1401.4, "identity": 343.6}
 # FP64-pipe instructions per ray-step (sm__inst_executed_pipe_fp64 x 32, same captures)
 FP64_PIPE_INST_PER_RAY_STEP = {"libm": 945.2, "identity": 283.6}
 # DRAM bytes (read + written) per ray-step of the plain kernel on the seamount
-# workload, from an ncu capture whose stored trajectory rows dwarf L2; None
-# until measured.
-K1_DRAM_BYTES_PER_RAY_STEP = None
-K1_DRAM_NOTE = ""
+# workload: ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch
+# over its 65,536 rays x 1,000 steps (55.5 MB read, 2,573.7 MB written: the
+# 2.62 GB of stored rows, 20x L2, less what L2 still held at the end).
+K1_DRAM_BYTES_PER_RAY_STEP = (55537408 + 2573673472) / (65536 * 1000)
+K1_DRAM_NOTE = ("ncu DRAM bytes of a 65,536-ray x 1,000-step launch of the same workload "
+                "(55.5 MB read, 2,573.7 MB written) scaled by ray-steps; rows still in L2 at the "
+                "end of that launch (at most 129 MB) are not counted")
 # The same for the batched kernel on the shelf-slope field.
 K2_SHELF_DRAM_BYTES_PER_RAY_STEP = None
 K2_SHELF_DRAM_NOTE = ""
@@ -119,6 +122,8 @@ def parse():
                    help="shelf-slope: rays of the endpoint-error comparison")
     p.add_argument("--ns-adjoint-calls", type=int, default=2,
                    help="differentiation case: timed forward and gradient calls per precision")
+    p.add_argument("--ns-only", action="store_true",
+                   help="print only the shelf-slope batched-vs-plain measurement (for profiling)")
     return p.parse_args()
 
 
@@ -543,20 +548,30 @@ def fp64_trajectories(b, c, rays, t0, dt, steps, dev, stream):
 
 def chunked_endpoint_errors(end, n_steps, traj, nr, per=512):
     """batch.endpoint_errors of end states against device trajectories,
-    `per` rays at a time (small host copies).  Returns (relative position
-    errors, direction errors, rays compared)."""
+    `per` rays at a time (small host copies).  Returns per-ray relative
+    position and direction errors (NaN where not compared)."""
     from mantaray_gb300.batch import endpoint_errors
 
     n = int(nr.numel())
-    rel, dth, compared = [], [], 0
+    rel, dth = [], []
     for s in range(0, n, per):
         e = slice(s, min(n, s + per))
         er = endpoint_errors(end[:, e], n_steps[e], traj[:, :, e].cpu().numpy(),
-                             nr[e].cpu().numpy())
+                             nr[e].cpu().numpy(), per_ray=True)
         rel.append(er["rel_position"])
         dth.append(er["direction"])
-        compared += er["compared"]
-    return np.concatenate(rel), np.concatenate(dth), compared
+    return np.concatenate(rel), np.concatenate(dth)
+
+
+def error_stats(rel, dth, mask=None):
+    """p50 / p99 / max of the compared rays' errors (optionally within mask)."""
+    m = np.isfinite(rel) & (True if mask is None else mask)
+    if not m.any():
+        return {"rays": 0}
+    r, d = rel[m], dth[m]
+    return {"rays": int(m.sum()), "rel_position_p50": float(np.median(r)),
+            "rel_position_p99": float(np.percentile(r, 99)), "rel_position_max": float(r.max()),
+            "direction_p99_rad": float(np.percentile(d, 99)), "direction_max_rad": float(d.max())}
 
 
 def last_finite_states(traj, nr):
@@ -633,14 +648,15 @@ def north_star_batched(args, dev, stream, flush) -> dict:
     stat_b = out.status[eidx].cpu().numpy()
     erays = [t[eidx] for t in ins]
     traj, nr = fp64_trajectories(b, c, erays, t0, dt, steps, dev, stream)
-    rel, dth, compared = chunked_endpoint_errors(end_b, nst_b, traj, nr)
+    rel, dth = chunked_endpoint_errors(end_b, nst_b, traj, nr)
     # the FP64 model's own sensitivity: the same rays started 1 cm further in x
     traj_p, nr_p = fp64_trajectories(b, c, [erays[0] + 0.01] + erays[1:], t0, dt, steps, dev,
                                      stream)
     end_p, last_p = last_finite_states(traj_p, nr_p)
     del traj_p
-    sens, _, _ = chunked_endpoint_errors(end_p, last_p, traj, nr)
+    sens, _ = chunked_endpoint_errors(end_p, last_p, traj, nr)
     del traj
+    cond = sens <= 1e-4  # rays whose FP64 endpoint is well-conditioned
 
     # the plain FP64 form's rate on a subset of the same rays, same horizon
     n_plain = min(args.ns_plain_rays, nominal)
@@ -684,18 +700,19 @@ def north_star_batched(args, dev, stream, flush) -> dict:
                                         "horizon, running rays continued, launches timed"},
         "batched_over_plain": value / plain, "target_batched_over_plain": ">= 5",
         "endpoint_error_vs_fp64": {
-            "rays": compared, "of": n_err,
+            "of": n_err,
             "status_counts": {"complete": int(status[0]), "out_of_domain": int(status[1]),
                               "dry": int(status[2]), "bad_wavenumber": int(status[3])},
-            "rel_position_p50": float(np.median(rel)),
-            "rel_position_p99": float(np.percentile(rel, 99)),
-            "rel_position_max": float(rel.max()),
-            "direction_p99_rad": float(np.percentile(dth, 99)),
-            "direction_max_rad": float(dth.max()), "target_rel_position": "<= 1e-3"},
+            "all_compared_rays": error_stats(rel, dth),
+            "fp64_conditioned_rays": dict(
+                error_stats(rel, dth, cond), share_of_rays=float(np.mean(cond)),
+                which="rays whose FP64 endpoint moves by <= 1e-4 of its path when the start "
+                      "moves 1 cm"),
+            "target_rel_position": "<= 1e-3"},
         "fp64_endpoint_change_for_1cm_start_shift": {
-            "rel_position_p50": float(np.median(sens)),
-            "rel_position_p99": float(np.percentile(sens, 99)),
-            "rel_position_max": float(sens.max())},
+            "rel_position_p50": float(np.nanmedian(sens)),
+            "rel_position_p99": float(np.nanpercentile(sens, 99)),
+            "rel_position_max": float(np.nanmax(sens))},
         "roofline": roof, "clocks": clock,
         "gpu_launches": args.ns_calls,
     }
@@ -1152,6 +1169,14 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", 0))
     if args.impl == "reference":
         reference_arm(args, rank, world)
+    elif args.ns_only:
+        import torch
+
+        torch.cuda.set_device(local_rank)
+        dev = torch.device("cuda", local_rank)
+        flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+        print(json.dumps(north_star_batched(args, dev, torch.cuda.current_stream(dev), flush)),
+              flush=True)
     elif args.form == "batched":
         batched_arm(args, rank, world, local_rank)
     elif args.form == "adjoint":

@@ -65,17 +65,19 @@ extern "C" {
  *   MR_STOP_STAGE1: the first-stage derivative of the step just taken.
  *   MR_STOP_FRESH:  the derivative evaluated at the new state.
  * Right-hand-side arithmetic of the plain FP64 kernel:
+ *   MR_MATH_IDENTITY: (default, 0) the reference's quantities from one
+ *                     expm1, one reciprocal, two rsqrt and kx/k, ky/k (exact
+ *                     identities, FMAs; a few ulps from the reference's
+ *                     calls), about 3x as fast on the FP64 pipe.
  *   MR_MATH_LIBM:     the reference's own calls (atan2, cos, sin, cosh, tanh,
- *                     sinh, three sqrt) in its own order.
- *   MR_MATH_IDENTITY: the same quantities from one expm1, one reciprocal,
- *                     two rsqrt and kx/k, ky/k (exact identities, FMAs; a
- *                     few ulps apart), about 4x as fast on the FP64 pipe.
- * Field lookups and interpolation are bit-identical to the reference in
- * both. */
+ *                     sinh, three sqrt) in its own order; reproduces the
+ *                     reference's single-step known answers to f64::EPSILON.
+ * Both hold every step within 1e-9 (relative) of the reference.  Field
+ * lookups and interpolation are bit-identical to the reference in both. */
 #define MR_STOP_STAGE1 0x0
 #define MR_STOP_FRESH 0x1
-#define MR_MATH_LIBM 0x0
-#define MR_MATH_IDENTITY 0x10
+#define MR_MATH_IDENTITY 0x0
+#define MR_MATH_LIBM 0x10
 
 typedef struct mr_bathymetry mr_bathymetry;
 typedef struct mr_current mr_current;

@@ -24,8 +24,8 @@ RAY_STOPPED = 1
 
 STOP_STAGE1 = 0x0
 STOP_FRESH = 0x1
-MATH_LIBM = 0x0
-MATH_IDENTITY = 0x10
+MATH_IDENTITY = 0x0
+MATH_LIBM = 0x10
 
 # Exported symbols (checked by the CPU test that loads the library).
 SYMBOLS = (

@@ -129,7 +129,8 @@ class BatchTracer:
                 return make_config(**stored[key])
         if candidates is None:
             candidates = [make_config(b, bps, rpl, 32, order)
-                          for b, bps, rpl, order in itertools.product((64, 128, 256), (2, 4, 8),
+                          for b, bps, rpl, order in itertools.product((64, 128, 256),
+                                                                      (2, 4, 6, 8, 12),
                                                                       (1, 2), (0, 1))
                           if b * bps <= 2048]
         out = self.alloc(int(x0.numel()), probe_steps, 0, device=x0.device)
@@ -200,13 +201,14 @@ class BatchGraph:
             pass
 
 
-def endpoint_errors(end_state, n_steps, oracle_traj, oracle_rows):
+def endpoint_errors(end_state, n_steps, oracle_traj, oracle_rows, per_ray=False):
     """Endpoint error of batched results against full-precision trajectories
     (traj[5][rows][n], e.g. the plain FP64 form's) at the batched form's last
     valid step: relative position error |dx| / path length (path length along
     the full-precision trajectory up to that step) and direction error
     |d theta| (rad).  Rays that the batched form carried past the
-    full-precision trajectory's last finite row are counted, not compared."""
+    full-precision trajectory's last finite row are counted, not compared.
+    per_ray: the error arrays hold every ray, NaN where not compared."""
     end = np.asarray(end_state)
     steps = np.asarray(n_steps).astype(np.int64)
     n = end.shape[1]
@@ -225,6 +227,10 @@ def endpoint_errors(end_state, n_steps, oracle_traj, oracle_rows):
     path = np.nansum(seg, axis=0)
     rel = np.where(path > 0, dxy / np.maximum(path, 1e-300), 0.0)
     dth = np.abs(np.angle(np.exp(1j * (np.arctan2(end[4], end[3]) - np.arctan2(oky, okx)))))
-    return {"rel_position": rel[cmp], "direction": dth[cmp], "compared": int(np.sum(cmp)),
+    if per_ray:
+        rel, dth = np.where(cmp, rel, np.nan), np.where(cmp, dth, np.nan)
+    else:
+        rel, dth = rel[cmp], dth[cmp]
+    return {"rel_position": rel, "direction": dth, "compared": int(np.sum(cmp)),
             "past_end": int(np.sum(~cmp)), "early_stop": int(np.sum(steps < last_finite)),
             "n": n}

@@ -86,12 +86,13 @@ def _f64(a):
 
 
 def trace(bathymetry: Bathymetry, current: Current, x0, y0, kx0, ky0, duration: float,
-          step_size: float, t0: float = 0.0, stop_rule="stage1", math="libm",
+          step_size: float, t0: float = 0.0, stop_rule="stage1", math="identity",
           out: np.ndarray | None = None, rows_cap: int | None = None) -> TraceResult:
     """Traces rays from t0 to t0 + duration with step `step_size` (plain FP64
-    kernel).  stop_rule: "stage1" or "fresh"; math: "libm" (the reference's
-    transcendental calls) or "identity" (same quantities, fewer FP64
-    instructions).  `out` may be a preallocated (page-locked for speed)
+    kernel).  stop_rule: "stage1" or "fresh"; math: "identity" (default: the
+    reference's quantities with fewer FP64 instructions) or "libm" (the
+    reference's transcendental calls in its order); both within 1e-9 of the
+    reference at every step.  `out` may be a preallocated (page-locked for speed)
     float64 array of shape (5, rows_cap, n)."""
     L = N.load()
     x0, y0, kx0, ky0 = (_f64(a) for a in (x0, y0, kx0, ky0))
@@ -116,7 +117,7 @@ def trace(bathymetry: Bathymetry, current: Current, x0, y0, kx0, ky0, duration: 
 
 def trace_device(bathymetry: Bathymetry, current: Current, x0, y0, kx0, ky0, t0: float,
                  t_end: float, step_size: float, traj, n_rows, status, stop_rule="stage1",
-                 math="libm", stream=None) -> None:
+                 math="identity", stream=None) -> None:
     """Device-buffer form: every array argument is a CUDA tensor (torch) or any
     object with `data_ptr()`; traj has shape (5, rows_cap, n).  Asynchronous on
     `stream` (a torch.cuda.Stream, a raw handle, or None for the current
@@ -143,15 +144,17 @@ def _open_fields(bathymetry, current):
 
 
 def single_ray(x0: float, y0: float, kx0: float, ky0: float, duration: float, step_size: float,
-               bathymetry, current, math: str = "libm"):
+               bathymetry, current, math: str = "identity"):
     """Propagates one ray (reference: python/mantaray/core.py:9-65).
 
     `bathymetry` / `current` are NetCDF-3 paths (variables x, y, depth and
     x, y, u, v, as src/ffi.rs:36-38 requires) or field objects.  Returns a
     dataset over `time_step` with variables time, x, y, kx, ky.  `math`
-    (not in the reference): "libm" evaluates the reference's expressions with
-    its transcendental calls, "identity" the same quantities with fewer FP64
-    instructions (about 4x faster; within 1e-9 of the reference as well)."""
+    (not in the reference): "identity" (default) evaluates the reference's
+    quantities with fewer FP64 instructions, "libm" its expressions with its
+    transcendental calls (about 3x slower; it also reproduces the reference's
+    single-step known answers to f64::EPSILON).  Both stay within 1e-9 of the
+    reference at every step."""
     b, c = _open_fields(bathymetry, current)
     res = trace(b, c, x0, y0, kx0, ky0, duration, step_size, math=math)
     rows = int(res.n_rows[0])
@@ -164,7 +167,7 @@ def single_ray(x0: float, y0: float, kx0: float, ky0: float, duration: float, st
 
 
 def ray_tracing(x0, y0, kx0, ky0, duration: float, step_size: float, bathymetry, current,
-                math: str = "libm"):
+                math: str = "identity"):
     """Traces many rays (reference: python/mantaray/core.py:68-132).
 
     Returns a dataset over (`time_step`, `ray`), rays shorter than the longest

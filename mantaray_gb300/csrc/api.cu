@@ -67,9 +67,10 @@ void free_mem(std::vector<void *> &mem) {
   mem.clear();
 }
 
-constexpr int kOptionsMask = MR_STOP_FRESH | MR_MATH_IDENTITY;
-// Options of the reference-shaped entry points (mr_single_ray, the file forms).
-constexpr int kDropInOptions = MR_STOP_STAGE1 | MR_MATH_LIBM;
+constexpr int kOptionsMask = MR_STOP_FRESH | MR_MATH_LIBM;
+// Options of the reference-shaped entry points (mr_single_ray, the file
+// forms): the default arithmetic, within 1e-9 of the reference like libm's.
+constexpr int kDropInOptions = MR_STOP_STAGE1 | MR_MATH_IDENTITY;
 
 // Keep freed stream-ordered allocations pooled across calls (set once per
 // device); mr_trace's staging buffers are then reused instead of remapped.
@@ -331,7 +332,7 @@ int launch(const mr_bathymetry *b, const mr_current *c, size_t n, const double *
   a.n_rows = n_rows;
   a.status = status;
   cudaError_t e = mr::launch_rk4_f64(b->dev, c->dev, a, options & MR_STOP_FRESH,
-                                     (options & MR_MATH_IDENTITY) != 0, stream);
+                                     (options & MR_MATH_LIBM) == 0, stream);
   if (e != cudaSuccess) return cuda_fail(e, "rk4_f64 launch");
   return MR_OK;
 }

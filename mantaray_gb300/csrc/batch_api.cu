@@ -43,6 +43,8 @@ int pack_bathy(mr_batch *b, const mr_bathymetry *h, mr::PackedGrid *g, cudaStrea
   if (!(h->dev.xspace > 0.0) || !(h->dev.yspace > 0.0))
     return fail(MR_ERR_INVALID_ARGUMENT, "the batched form needs ascending, evenly spaced axes");
   const size_t ncell = (h->dev.nx - 1) * (h->dev.ny - 1);
+  if (ncell > 0x7fffffffull)
+    return fail(MR_ERR_INVALID_ARGUMENT, "the batched form indexes fewer than 2^31 cells");
   void *cells = nullptr;
   MR_CUDA(cudaMalloc(&cells, ncell * 2 * sizeof(float4)));
   b->mem.push_back(cells);
@@ -82,6 +84,8 @@ int pack_current(mr_batch *b, const mr_current *c, mr::PackedGrid *g, cudaStream
   if (!(c->dev.xspace > 0.0) || !(c->dev.yspace > 0.0))
     return fail(MR_ERR_INVALID_ARGUMENT, "the batched form needs ascending, evenly spaced axes");
   const size_t ncell = (c->dev.nx - 1) * (c->dev.ny - 1);
+  if (ncell > 0x7fffffffull)
+    return fail(MR_ERR_INVALID_ARGUMENT, "the batched form indexes fewer than 2^31 cells");
   void *cells = nullptr;
   MR_CUDA(cudaMalloc(&cells, ncell * 3 * sizeof(float4)));
   b->mem.push_back(cells);

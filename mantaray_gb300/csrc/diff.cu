@@ -266,27 +266,28 @@ struct NodeAcc {
 
 // Adds `vals[4]` to nodes (base, base+1, base+nx, base+nx+1) of `arr` in
 // FP64, summed first across the active lanes of the warp that flush the same
-// base.
+// base.  Each group's lowest lane (its leader) adds its peers' values in
+// ascending lane order; the loop runs once per member of the largest group
+// (all active lanes take part in every shuffle, each reading the next member
+// of its own group), so lanes flushing distinct cells cost no shuffle at all.
 template <typename T>
 __device__ __forceinline__ void scatter4(double *arr, int64_t base, int nx, const T vals[4]) {
   const unsigned active = __activemask();
   const unsigned peers = __match_any_sync(active, base);
   const int lane = threadIdx.x & 31;
   const int leader = __ffs(peers) - 1;
-  const bool shared = __any_sync(active, __popc(peers) > 1);
+  const unsigned largest = __reduce_max_sync(active, static_cast<unsigned>(__popc(peers)));
   double v[4] = {double(vals[0]), double(vals[1]), double(vals[2]), double(vals[3])};
-  if (shared) {
-    // every active lane takes part in each shuffle; a group's leader keeps
-    // the values of its peers
-    for (int src = 0; src < 32; ++src) {
-      if (!((active >> src) & 1u)) continue;
-      T o[4];
+  unsigned rest = peers & (peers - 1u);  // the group without its leader
+  for (unsigned it = 1; it < largest; ++it) {
+    const int src = rest ? __ffs(rest) - 1 : lane;
+    rest &= rest - 1u;
+    T o[4];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) o[q] = __shfl_sync(active, vals[q], src);
-      if (lane == leader && src != lane && ((peers >> src) & 1u)) {
+    for (int q = 0; q < 4; ++q) o[q] = __shfl_sync(active, vals[q], src);
+    if (lane == leader && src != lane) {
 #pragma unroll
-        for (int q = 0; q < 4; ++q) v[q] += double(o[q]);
-      }
+      for (int q = 0; q < 4; ++q) v[q] += double(o[q]);
     }
   }
   if (lane == leader) {

@@ -22,6 +22,51 @@ namespace {
 constexpr unsigned kFull = 0xffffffffu;
 constexpr float kGf = 9.8f;
 
+// Single-precision approximations of the special-function unit (PTX ISA:
+// rcp.approx has at most 1 ulp of error, rsqrt.approx and ex2.approx a
+// relative error near 2^-22), with subnormal inputs and results flushed to
+// zero.  The same instruction in every build gives the same bits in every
+// build, whatever its -ftz setting.
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float rsqrt_approx(float x) {
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float ex2_approx(float x) {
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// m = 1 - exp(x) and q = exp(x) for x = -2kh <= 0.  Below -0.5, exp(x) is at
+// most 0.61, so 1 - exp(x) keeps its relative accuracy: q = 2^(x log2 e) on
+// the special-function unit.  From -0.5 to 0, m = -(e^x - 1) by the Taylor
+// series of e^x - 1 to the x^8 / 8! term, evaluated by Horner's rule (the
+// remainder is below 0.5^9 / 9! = 5.4e-9, relative 1.4e-8 at x = -0.5 and
+// smaller toward 0), so m stays relatively accurate in shallow water where
+// it tends to 2kh.
+__device__ __forceinline__ void one_minus_exp(float x, float &m, float &q) {
+  if (x < -0.5f) {
+    q = ex2_approx(x * 1.44269504088896341f);
+    m = 1.0f - q;
+  } else {
+    float p = fmaf(x, 1.0f / 40320.0f, 1.0f / 5040.0f);
+    p = fmaf(x, p, 1.0f / 720.0f);
+    p = fmaf(x, p, 1.0f / 120.0f);
+    p = fmaf(x, p, 1.0f / 24.0f);
+    p = fmaf(x, p, 1.0f / 6.0f);
+    p = fmaf(x, p, 0.5f);
+    p = fmaf(x, p, 1.0f);
+    m = -(x * p);
+    q = 1.0f - m;
+  }
+}
+
 // Position of a lane on one grid: the cell of its origin (integral floats:
 // exact, grids have fewer than 2^24 points per axis) plus the origin's
 // fractional cell offset.
@@ -45,37 +90,23 @@ __device__ __forceinline__ GridPos grid_pos(const PackedGrid &g, double ox, doub
 }
 
 // Cell index and in-cell fractions at offset (px, py) from the origin; false
-// when outside the grid's cells.  The cell's coordinates are integral floats
-// (exact sums), tested against the grid's bounds and converted once.
+// when outside the grid's cells (or at a NaN position), and the index is then
+// meaningless.  The cell's coordinates are integral floats (exact sums),
+// tested against the grid's bounds.  Cells are indexed in 32 bits (the
+// batch refuses grids of 2^31 cells or more).
 __device__ __forceinline__ bool locate(const PackedGrid &g, const GridPos &p, float px, float py,
-                                       int64_t *cell, float *fx, float *fy) {
+                                       int *cell, float *fx, float *fy) {
   const float ux = fmaf(px, g.inv_sp_x, p.f0);
   const float uy = fmaf(py, g.inv_sp_y, p.g0);
   const float flx = floorf(ux), fly = floorf(uy);
   const float cx = p.fi0 + flx, cy = p.fj0 + fly;
-  if (!(cx >= 0.0f && cx <= g.cx_max && cy >= 0.0f && cy <= g.cy_max)) return false;
-  *cell = static_cast<int64_t>(static_cast<int>(cy)) * (g.nx - 1) + static_cast<int>(cx);
+  // saturating conversions and unsigned arithmetic: defined for any position
+  *cell = static_cast<int>(static_cast<unsigned>(__float2int_rz(cy)) *
+                               static_cast<unsigned>(g.nx - 1) +
+                           static_cast<unsigned>(__float2int_rz(cx)));
   *fx = ux - flx;
   *fy = uy - fly;
-  return true;
-}
-
-// locate for the branch-free right-hand side: the same cell and fractions
-// inside the grid; outside it (or at a NaN position) returns false with the
-// cell clamped into the grid, so that its record can be read all the same.
-__device__ __forceinline__ bool locate_clamped(const PackedGrid &g, const GridPos &p, float px,
-                                               float py, int64_t *cell, float *fx, float *fy) {
-  const float ux = fmaf(px, g.inv_sp_x, p.f0);
-  const float uy = fmaf(py, g.inv_sp_y, p.g0);
-  const float flx = floorf(ux), fly = floorf(uy);
-  const float cx = p.fi0 + flx, cy = p.fj0 + fly;
-  const bool inside = cx >= 0.0f && cx <= g.cx_max && cy >= 0.0f && cy <= g.cy_max;
-  // fmaxf(NaN, 0) is 0: a NaN coordinate clamps too
-  const float kx = fminf(fmaxf(cx, 0.0f), g.cx_max), ky = fminf(fmaxf(cy, 0.0f), g.cy_max);
-  *cell = static_cast<int64_t>(static_cast<int>(ky)) * (g.nx - 1) + static_cast<int>(kx);
-  *fx = ux - flx;
-  *fy = uy - fly;
-  return inside;
+  return cx >= 0.0f && cx <= g.cx_max && cy >= 0.0f && cy <= g.cy_max;
 }
 
 // c = the cell's bilinear coefficients (batch.h): c.x + c.y fx + c.z fy +
@@ -88,7 +119,7 @@ __device__ __forceinline__ float bilin(const float4 &c, float fx, float fy) {
 // cell for several steps, so most stage lookups reuse them instead of
 // loading them again (same values, no memory latency on the dependent chain).
 struct CellCache {
-  int64_t bkey, ckey;     // cell indices held, -1: none
+  int bkey, ckey;         // cell indices held, -1: none
   float4 b0;              // depth's bilinear coefficients
   float bx, by;           // dh/dx, dh/dy
   float4 c0, c1, c2;      // u's and v's coefficients, the current's gradients
@@ -101,69 +132,34 @@ struct RayLane {
   GridPos pb, pc;   // origin on the bathymetry and current grids
   float px, py, kx, ky;      // offsets and wavenumber
   float cpx, cpy, ckx, cky;  // Kahan compensations
-  int64_t step;
+  int32_t step;       // steps taken (max_steps < 2^31)
   int32_t saved;
   int32_t to_save;    // steps until the next decimated row (no 64-bit modulo per step)
   int32_t to_rebase;  // steps until the next origin rebase
   CellCache cache;
 };
 
-// The fields at offset (px, py) in the bathymetry cell cb (fractions fx,
-// fy), with any current: constant, gridded on the same grid, or gridded on
-// its own grid.  Returns a BatchStatus (BATCH_COMPLETE: found).
-__device__ __forceinline__ int lookup_fields(const ScenarioDev &s, RayLane &L, float px, float py,
-                                             int64_t cb, float fx, float fy, float &h, float &u,
-                                             float &v, float &dudx, float &dudy, float &dvdx,
-                                             float &dvdy) {
-  CellCache &C = L.cache;
-  if (cb != C.bkey) {
-    C.b0 = __ldg(s.bathy.cells + 2 * cb);
-    const float4 b1 = __ldg(s.bathy.cells + 2 * cb + 1);
-    C.bx = b1.x;
-    C.by = b1.y;
-    C.bkey = cb;
-  }
-  h = bilin(C.b0, fx, fy);
-  dudx = dudy = dvdx = dvdy = 0.0f;
-  if (s.current.kind == 0) {
-    int64_t cc = cb;
-    float gx = fx, gy = fy;  // the same cell when the grids coincide (same origin, same arithmetic)
-    if (!s.same_grid && !locate(s.current, L.pc, px, py, &cc, &gx, &gy))
-      return BATCH_OUT_OF_DOMAIN;
-    if (cc != C.ckey) {
-      C.c0 = __ldg(s.current.cells + 3 * cc);
-      C.c1 = __ldg(s.current.cells + 3 * cc + 1);
-      C.c2 = __ldg(s.current.cells + 3 * cc + 2);
-      C.ckey = cc;
-    }
-    u = bilin(C.c0, gx, gy);
-    v = bilin(C.c1, gx, gy);
-    dudx = C.c2.x; dudy = C.c2.y; dvdx = C.c2.z; dvdy = C.c2.w;
-  } else {
-    u = s.current.cu;
-    v = s.current.cv;
-  }
-  return BATCH_COMPLETE;
-}
-
 // The ray equations in FP32 from the looked-up fields (bx, by: dh/dx,
-// dh/dy): the identity form of the right-hand side in single precision.
+// dh/dy): the identity form of the right-hand side in single precision,
+// with a = kh, q = exp(-2a), m = 1 - q:
+//   tanh a = m / (2 - m),  a / cosh^2 a = 4 a q / (2 - m)^2,
+//   1 / (sinh a cosh a) = 4 q / (m (2 - m)),
+//   c_g = (g/2) (tanh a + a / cosh^2 a) / sqrt(g k tanh a),
+//   dk/dt from the depth = -(k/2) sqrt(g k tanh a) / (sinh a cosh a) grad h.
 __device__ __forceinline__ void ray_equations(float h, float u, float v, float dudx, float dudy,
                                               float dvdx, float dvdy, float bx, float by,
-                                              float kx, float ky, float d[4]) {
-  const float k2 = fmaf(kx, kx, ky * ky);
-  const float rk = rsqrtf(k2);
+                                              float kx, float ky, float k2, float d[4]) {
+  const float rk = rsqrt_approx(k2);
   const float k = k2 * rk;
   const float kh = k * h;
-  const float m = -expm1f(-2.0f * kh);  // 1 - exp(-2kh)
-  const float q = 1.0f - m;
-  const float inv_d = __frcp_rn(m * (2.0f - m));  // = 1.0f / x, correctly rounded
+  float m, q;
+  one_minus_exp(-2.0f * kh, m, q);
+  const float inv_d = rcp_approx(m * (2.0f - m));  // 1 / (m (2 - m))
   const float r = m * inv_d;            // 1 / (2 - m)
   const float th = m * r;               // tanh(kh)
   const float gkt = kGf * k * th;
-  const float rs = rsqrtf(gkt);
+  const float rs = rsqrt_approx(gkt);
   const float q4 = 4.0f * q;
-  // kh / cosh^2(kh) = 4 kh q r^2 and 1 / (sinh(kh) cosh(kh)) = 4 q inv_d
   const float cg = (0.5f * kGf) * (fmaf(kh * q4, r * r, th) * rs);
   const float f = (-0.5f * k) * ((q4 * inv_d) * (gkt * rs));
   const float cgk = cg * rk;            // c_g / k: c_g cos(theta) = cgk kx
@@ -173,75 +169,90 @@ __device__ __forceinline__ void ray_equations(float h, float u, float v, float d
   d[3] = fmaf(-ky, dvdy, fmaf(-kx, dudy, f * by));
 }
 
-// The status of a right-hand side from the looked-up depth and the
-// wavenumber: dry (h <= 0), out of domain (h NaN: a cell past the depth
-// array), bad wavenumber (k^2 not in (0, 3e38)), else complete.
-__device__ __forceinline__ int field_status(float h, float kx, float ky) {
-  if (!(h > 0.0f)) return h <= 0.0f ? BATCH_DRY : BATCH_OUT_OF_DOMAIN;
-  const float k2 = fmaf(kx, kx, ky * ky);
-  if (!(k2 > 0.0f && k2 < 3.0e38f)) return BATCH_BAD_WAVENUMBER;
-  return BATCH_COMPLETE;
-}
-
-// The record of cell cb of both fields when the current is gridded on the
-// bathymetry's grid (modes 2 and 3), unless the lane holds it already.
-__device__ __forceinline__ void load_same_grid_cell(const ScenarioDev &s, CellCache &C,
-                                                    int64_t cb) {
+// The records of bathymetry cell cb, unless the lane holds them.
+__device__ __forceinline__ void load_bathy_cell(const ScenarioDev &s, CellCache &C, int cb) {
   if (cb != C.bkey) {
-    C.b0 = __ldg(s.bathy.cells + 2 * cb);
-    const float4 b1 = __ldg(s.bathy.cells + 2 * cb + 1);
+    C.b0 = __ldg(s.bathy.cells + static_cast<int64_t>(cb) * 2);
+    const float4 b1 = __ldg(s.bathy.cells + static_cast<int64_t>(cb) * 2 + 1);
     C.bx = b1.x;
     C.by = b1.y;
-    C.c0 = __ldg(s.current.cells + 3 * cb);
-    C.c1 = __ldg(s.current.cells + 3 * cb + 1);
-    C.c2 = __ldg(s.current.cells + 3 * cb + 2);
     C.bkey = cb;
   }
 }
 
-// Right-hand side of modes 2 and 3 without early returns: the same values
-// and statuses as rhs_f32, with d always written (meaningless unless the
-// status is BATCH_COMPLETE), so that the four stages of a step need no
-// branches between them.  Only the cell-record load is conditional.
-__device__ __forceinline__ int rhs_f32_flat(const ScenarioDev &s, RayLane &L, float px, float py,
-                                            float kx, float ky, float d[4]) {
-  int64_t cb;
-  float fx, fy;
-  const bool inside = locate_clamped(s.bathy, L.pb, px, py, &cb, &fx, &fy);
-  CellCache &C = L.cache;
-  load_same_grid_cell(s, C, cb);
-  const float h = bilin(C.b0, fx, fy);
-  const int st = inside ? field_status(h, kx, ky) : BATCH_OUT_OF_DOMAIN;
-  ray_equations(h, bilin(C.c0, fx, fy), bilin(C.c1, fx, fy), C.c2.x, C.c2.y, C.c2.z, C.c2.w,
-                C.bx, C.by, kx, ky, d);
-  return st;
+// The records of current cell cc, unless the lane holds them.
+__device__ __forceinline__ void load_current_cell(const ScenarioDev &s, CellCache &C, int cc) {
+  if (cc != C.ckey) {
+    C.c0 = __ldg(s.current.cells + static_cast<int64_t>(cc) * 3);
+    C.c1 = __ldg(s.current.cells + static_cast<int64_t>(cc) * 3 + 1);
+    C.c2 = __ldg(s.current.cells + static_cast<int64_t>(cc) * 3 + 2);
+    C.ckey = cc;
+  }
 }
 
-// Right-hand side in FP32 at offset (px, py); returns a BatchStatus.
-// MODE 2 and 3: the current is gridded on the bathymetry's grid, so one cell
-// (one key, one test) serves both fields; otherwise lookup_fields handles
-// any current.
-template <int MODE>
+// The records of cell cb of both fields when the current is gridded on the
+// bathymetry's grid (modes 2 and 3), unless the lane holds them.
+__device__ __forceinline__ void load_same_grid_cell(const ScenarioDev &s, CellCache &C, int cb) {
+  if (cb != C.bkey) {
+    C.b0 = __ldg(s.bathy.cells + static_cast<int64_t>(cb) * 2);
+    const float4 b1 = __ldg(s.bathy.cells + static_cast<int64_t>(cb) * 2 + 1);
+    C.bx = b1.x;
+    C.by = b1.y;
+    C.c0 = __ldg(s.current.cells + static_cast<int64_t>(cb) * 3);
+    C.c1 = __ldg(s.current.cells + static_cast<int64_t>(cb) * 3 + 1);
+    C.c2 = __ldg(s.current.cells + static_cast<int64_t>(cb) * 3 + 2);
+    C.bkey = cb;
+  }
+}
+
+// One right-hand side in FP32 at offset (px, py), wavenumber (kx, ky).
+// The fields come from the lane's cell records (loaded when the lane does not
+// hold the cell; a point outside a grid loads nothing and uses the records
+// held, whatever they are).  With EXACT, returns the stage's BatchStatus: out
+// of domain (outside a grid, or depth NaN: a cell past the depth array), dry
+// (depth <= 0), bad wavenumber (k^2 not in (0, 3e38)), else complete;
+// without, BATCH_COMPLETE or not (the same test, no status code).  d is
+// meaningful only when complete.  Written without early returns so that the
+// four stages of a step run with no branch between them.  MODE 2 and 3: the
+// current is gridded on the bathymetry's grid, so one cell (one key, one
+// test) serves both fields.
+template <int MODE, bool EXACT>
 __device__ __forceinline__ int rhs_f32(const ScenarioDev &s, RayLane &L, float px, float py,
                                        float kx, float ky, float d[4]) {
-  int64_t cb;
-  float fx, fy;
-  if (!locate(s.bathy, L.pb, px, py, &cb, &fx, &fy)) return BATCH_OUT_OF_DOMAIN;
   CellCache &C = L.cache;
-  float h, u, v, dudx, dudy, dvdx, dvdy;
+  int cb;
+  float fx, fy;
+  bool inside = locate(s.bathy, L.pb, px, py, &cb, &fx, &fy);
+  float u, v, dudx, dudy, dvdx, dvdy;
   if (MODE == 2 || MODE == 3) {
-    load_same_grid_cell(s, C, cb);
-    h = bilin(C.b0, fx, fy);
+    load_same_grid_cell(s, C, inside ? cb : C.bkey);
     u = bilin(C.c0, fx, fy);
     v = bilin(C.c1, fx, fy);
     dudx = C.c2.x; dudy = C.c2.y; dvdx = C.c2.z; dvdy = C.c2.w;
   } else {
-    if (const int st = lookup_fields(s, L, px, py, cb, fx, fy, h, u, v, dudx, dudy, dvdx, dvdy))
-      return st;
+    load_bathy_cell(s, C, inside ? cb : C.bkey);
+    if (s.current.kind == 0) {
+      int cc = cb;
+      float gx = fx, gy = fy;  // the same cell when the grids coincide (same origin, same arithmetic)
+      if (!s.same_grid) inside &= locate(s.current, L.pc, px, py, &cc, &gx, &gy);
+      load_current_cell(s, C, inside ? cc : C.ckey);
+      u = bilin(C.c0, gx, gy);
+      v = bilin(C.c1, gx, gy);
+      dudx = C.c2.x; dudy = C.c2.y; dvdx = C.c2.z; dvdy = C.c2.w;
+    } else {
+      u = s.current.cu;
+      v = s.current.cv;
+      dudx = dudy = dvdx = dvdy = 0.0f;
+    }
   }
-  if (const int st = field_status(h, kx, ky)) return st;
-  ray_equations(h, u, v, dudx, dudy, dvdx, dvdy, C.bx, C.by, kx, ky, d);
-  return BATCH_COMPLETE;
+  const float h = bilin(C.b0, fx, fy);
+  const float k2 = fmaf(kx, kx, ky * ky);
+  ray_equations(h, u, v, dudx, dudy, dvdx, dvdy, C.bx, C.by, kx, ky, k2, d);
+  const bool wet = h > 0.0f, kok = k2 > 0.0f && k2 < 3.0e38f;
+  if (!EXACT) return (inside && wet && kok) ? BATCH_COMPLETE : BATCH_OUT_OF_DOMAIN;
+  if (inside && wet && kok) return BATCH_COMPLETE;
+  if (!inside || (!(h <= 0.0f) && !wet)) return BATCH_OUT_OF_DOMAIN;
+  return !wet ? BATCH_DRY : BATCH_BAD_WAVENUMBER;
 }
 
 __device__ __forceinline__ void kahan_add(float &sum, float &comp, float inc) {
@@ -277,7 +288,7 @@ __device__ __forceinline__ void finish(const BatchArgs &a, RayLane &L, int statu
   a.end_state[2 * a.n_stride + r] = L.oy + (static_cast<double>(L.py) - static_cast<double>(L.cpy));
   a.end_state[3 * a.n_stride + r] = static_cast<double>(L.kx) - static_cast<double>(L.ckx);
   a.end_state[4 * a.n_stride + r] = static_cast<double>(L.ky) - static_cast<double>(L.cky);
-  a.n_steps[r] = static_cast<int32_t>(L.step);
+  a.n_steps[r] = L.step;
   a.n_saved[r] = L.saved;
   a.status[r] = static_cast<uint8_t>(status);
   L.ray = -1;
@@ -312,7 +323,11 @@ __device__ __forceinline__ void start(const BatchArgs &a, RayLane &L, int64_t r)
   L.pc = s.same_grid ? L.pb : grid_pos(s.current, L.ox, L.oy);
   L.step = 0;
   L.saved = 0;
-  L.cache.bkey = L.cache.ckey = -1;
+  // no cell held; the records are defined values until the first load
+  CellCache &C = L.cache;
+  C.bkey = C.ckey = -1;
+  C.b0 = C.c0 = C.c1 = C.c2 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  C.bx = C.by = 0.0f;
   L.to_save = save_period(a);
   L.to_rebase = a.rebase_interval;
   if (a.decimation > 0) {
@@ -321,12 +336,35 @@ __device__ __forceinline__ void start(const BatchArgs &a, RayLane &L, int64_t r)
   }
 }
 
+// The status of a step whose four stages did not all succeed: the stages
+// again, in order, up to the first that fails (the same arithmetic on the
+// same inputs, so the same values and the same first failure).  Taken once
+// per ray at most: the ray ends there.  One stage in a loop: little code.
+template <int MODE>
+__device__ __forceinline__ int step_status(const ScenarioDev &s, RayLane &L, float dt,
+                                           float half) {
+  float k[4], x[4] = {L.px, L.py, L.kx, L.ky};
+#pragma unroll 1
+  for (int st = 0; st < 4; ++st) {
+    const int r = rhs_f32<MODE, true>(s, L, x[0], x[1], x[2], x[3], k);
+    if (r != BATCH_COMPLETE) return r;
+    const float w = st == 2 ? dt : half;
+    x[0] = fmaf(w, k[0], L.px);
+    x[1] = fmaf(w, k[1], L.py);
+    x[2] = fmaf(w, k[2], L.kx);
+    x[3] = fmaf(w, k[3], L.ky);
+  }
+  // not reached: the same four stages failed a moment ago.  Ending the ray
+  // all the same keeps every ray's step count bounded.
+  return BATCH_OUT_OF_DOMAIN;
+}
+
 // One RK4 step of lane L.  Returns BATCH_COMPLETE while the ray goes on.
-// FLAT (modes 2 and 3 only): the four stages without branches between them
-// (rhs_f32_flat), which needs more registers: the uncapped build takes it
-// (65,536-ray seamount 33.6 -> 35.7 G ray-steps/s), the 72-register build
-// does not (it spilled: 4,096^2 shelf-slope 50.1 -> 47.3 G).
-template <int MODE, bool FLAT>
+// The four stages run without branches between them (each stage's status is
+// a value, tested once for all four); a failed step is redone by step_status
+// for the status of its first failing stage, and the ray keeps the state it
+// had before the step.
+template <int MODE>
 __device__ __forceinline__ int advance(const BatchArgs &a, RayLane &L) {
   const ScenarioDev &s = scenario<MODE>(a, L.scen);
   // step constants in FP32 from the host (a conversion here would run on the
@@ -334,31 +372,14 @@ __device__ __forceinline__ int advance(const BatchArgs &a, RayLane &L) {
   const float dt = a.dt_f;
   const float half = a.half_f;
   float k1[4], k2[4], k3[4], k4[4];
-  int st;
-  if (FLAT && (MODE == 2 || MODE == 3)) {
-    // all four stages, then the first stage's failure (a failed stage's
-    // derivative only feeds stages whose results are dropped)
-    st = rhs_f32_flat(s, L, L.px, L.py, L.kx, L.ky, k1);
-    const int s2 = rhs_f32_flat(s, L, fmaf(half, k1[0], L.px), fmaf(half, k1[1], L.py),
-                                fmaf(half, k1[2], L.kx), fmaf(half, k1[3], L.ky), k2);
-    const int s3 = rhs_f32_flat(s, L, fmaf(half, k2[0], L.px), fmaf(half, k2[1], L.py),
-                                fmaf(half, k2[2], L.kx), fmaf(half, k2[3], L.ky), k3);
-    const int s4 = rhs_f32_flat(s, L, fmaf(dt, k3[0], L.px), fmaf(dt, k3[1], L.py),
-                                fmaf(dt, k3[2], L.kx), fmaf(dt, k3[3], L.ky), k4);
-    st = st != BATCH_COMPLETE ? st : s2 != BATCH_COMPLETE ? s2 : s3 != BATCH_COMPLETE ? s3 : s4;
-  } else {
-    st = rhs_f32<MODE>(s, L, L.px, L.py, L.kx, L.ky, k1);
-    if (st == BATCH_COMPLETE)
-      st = rhs_f32<MODE>(s, L, fmaf(half, k1[0], L.px), fmaf(half, k1[1], L.py),
-                         fmaf(half, k1[2], L.kx), fmaf(half, k1[3], L.ky), k2);
-    if (st == BATCH_COMPLETE)
-      st = rhs_f32<MODE>(s, L, fmaf(half, k2[0], L.px), fmaf(half, k2[1], L.py),
-                         fmaf(half, k2[2], L.kx), fmaf(half, k2[3], L.ky), k3);
-    if (st == BATCH_COMPLETE)
-      st = rhs_f32<MODE>(s, L, fmaf(dt, k3[0], L.px), fmaf(dt, k3[1], L.py),
-                         fmaf(dt, k3[2], L.kx), fmaf(dt, k3[3], L.ky), k4);
-  }
-  if (st != BATCH_COMPLETE) return st;
+  const int s1 = rhs_f32<MODE, false>(s, L, L.px, L.py, L.kx, L.ky, k1);
+  const int s2 = rhs_f32<MODE, false>(s, L, fmaf(half, k1[0], L.px), fmaf(half, k1[1], L.py),
+                               fmaf(half, k1[2], L.kx), fmaf(half, k1[3], L.ky), k2);
+  const int s3 = rhs_f32<MODE, false>(s, L, fmaf(half, k2[0], L.px), fmaf(half, k2[1], L.py),
+                               fmaf(half, k2[2], L.kx), fmaf(half, k2[3], L.ky), k3);
+  const int s4 = rhs_f32<MODE, false>(s, L, fmaf(dt, k3[0], L.px), fmaf(dt, k3[1], L.py),
+                               fmaf(dt, k3[2], L.kx), fmaf(dt, k3[3], L.ky), k4);
+  if ((s1 | s2 | s3 | s4) != BATCH_COMPLETE) return step_status<MODE>(s, L, dt, half);
   const float sixth = a.sixth_f;
 #pragma unroll
   for (int q = 0; q < 4; ++q) k1[q] = sixth * fmaf(2.0f, k2[q] + k3[q], k1[q] + k4[q]);
@@ -379,11 +400,12 @@ __device__ __forceinline__ int advance(const BatchArgs &a, RayLane &L) {
   return BATCH_COMPLETE;
 }
 
-template <int RPT, int MODE, bool FLAT>
+template <int RPT, int MODE>
 __device__ __forceinline__ void k2_body(const BatchArgs &a) {
   const int lane = threadIdx.x & 31;
   const unsigned lt_mask = (1u << lane) - 1u;
   const int64_t n = a.n;
+  const int32_t max_steps = static_cast<int32_t>(a.max_steps);
   RayLane L[RPT];
 #pragma unroll
   for (int j = 0; j < RPT; ++j) L[j].ray = -1;
@@ -411,11 +433,11 @@ __device__ __forceinline__ void k2_body(const BatchArgs &a) {
 #pragma unroll
     for (int j = 0; j < RPT; ++j) {
       if (L[j].ray < 0) continue;
-      if (L[j].step >= a.max_steps) {
+      if (L[j].step >= max_steps) {
         finish(a, L[j], BATCH_COMPLETE);
         continue;
       }
-      const int st = advance<MODE, FLAT>(a, L[j]);
+      const int st = advance<MODE>(a, L[j]);
       if (st != BATCH_COMPLETE) finish(a, L[j], st);
     }
   }
@@ -438,14 +460,12 @@ __device__ __forceinline__ void k2_body(const BatchArgs &a) {
 // lookup); 2 is mode 1 and 3 is mode 0 with the current gridded on the
 // bathymetry's grid (every scenario's, for 3).
 template <int MODE>
-__global__ void __launch_bounds__(256) rk4_f32_kernel_1(BatchArgs a) {
-  k2_body<1, MODE, true>(a);
-}
+__global__ void __launch_bounds__(256) rk4_f32_kernel_1(BatchArgs a) { k2_body<1, MODE>(a); }
 template <int MODE>
-__global__ void __maxnreg__(72) rk4_f32_kernel_1r(BatchArgs a) { k2_body<1, MODE, false>(a); }
+__global__ void __maxnreg__(72) rk4_f32_kernel_1r(BatchArgs a) { k2_body<1, MODE>(a); }
 // Two rays per lane hold twice the lane state: no cap.
 template <int MODE>
-__global__ void __launch_bounds__(256) rk4_f32_kernel_2(BatchArgs a) { k2_body<2, MODE, false>(a); }
+__global__ void __launch_bounds__(256) rk4_f32_kernel_2(BatchArgs a) { k2_body<2, MODE>(a); }
 
 }  // namespace
 

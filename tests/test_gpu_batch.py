@@ -363,12 +363,31 @@ def test_edge_rays_get_their_status(mr):
     assert out.n_steps.numel() == 0
 
 
+def fp64_conditioning(oracle, ob, oc, x0, y0, kx0, ky0, t0, t_end, dt, o):
+    """Per ray, the FP64 endpoint's own relative change (as endpoint_errors
+    measures it) when the ray starts 1 cm further along x; NaN where the two
+    FP64 trajectories end at different steps."""
+    from mantaray_gb300.batch import endpoint_errors
+
+    p = oracle.trace(ob, oc, np.asarray(x0) + 0.01, y0, kx0, ky0, t0, t_end, dt)
+    n = p[1].size
+    ii = np.arange(n)
+    last = p[1].astype(np.int64) - 1
+    last = np.where(np.all(np.isfinite(p[0][1:, last, ii]), axis=0), last, np.maximum(last - 1, 0))
+    return endpoint_errors(p[0][:, last, ii], last, o[0], o[1], per_ray=True)["rel_position"]
+
+
 @pytest.mark.parametrize("size", ["fine_corner", "whole_domain"])
 def test_shelf_slope_against_oracle(mr, oracle, size):
     # The large single-scenario case's generator at test size (as in the
     # plain form's parity test): the batched FP32 end states against the
     # oracle's trajectories of the same rays, and the same rays through a
-    # captured graph give the same bits as the direct call.
+    # captured graph give the same bits as the direct call.  Over the whole
+    # domain the FP64 model itself turns chaotic on the rough shelf (a 1 cm
+    # start shift moves 1% of the endpoints by more than 1e-2 of their path
+    # at 20,000 steps, and none by more than 3e-6 at 10,000): the bar then
+    # applies to the rays whose FP64 endpoint a 1 cm shift moves by at most
+    # 1e-4, at least 85% of them (91% measured).
     from mantaray_gb300.batch import BatchTracer, endpoint_errors
     from mantaray_gb300.workloads import shelf_slope
 
@@ -382,10 +401,18 @@ def test_shelf_slope_against_oracle(mr, oracle, size):
     res = tracer.trace(*ins, r["dt"], r["steps"], t0=r["t0"])
     ob = oracle.Bathymetry.grid(f[0], f[1], f[2])
     oc = oracle.Current.grid(f[3], f[4], f[5], f[6])
-    o = oracle.trace(ob, oc, r["x0"], r["y0"], r["kx0"], r["ky0"], r["t0"],
-                     r["t0"] + r["steps"] * r["dt"], r["dt"])
+    t_end = r["t0"] + r["steps"] * r["dt"]
+    rays = (r["x0"], r["y0"], r["kx0"], r["ky0"])
+    o = oracle.trace(ob, oc, *rays, r["t0"], t_end, r["dt"])
     end, nst = res.end_state.cpu().numpy(), res.n_steps.cpu().numpy()
-    check_errors(endpoint_errors(end, nst, o[0], o[1]), size)
+    if size == "fine_corner":
+        check_errors(endpoint_errors(end, nst, o[0], o[1]), size)
+    else:
+        sens = fp64_conditioning(oracle, ob, oc, *rays, r["t0"], t_end, r["dt"], o)
+        cond = sens <= 1e-4
+        assert cond.mean() >= 0.85, cond.mean()
+        e = endpoint_errors(end[:, cond], nst[cond], o[0][:, :, cond], o[1][cond])
+        check_errors(e, size)
     g = tracer.graph(*ins, r["dt"], r["steps"], t0=r["t0"])
     g.launch()
     np.testing.assert_array_equal(g.out.end_state.cpu().numpy(), end)

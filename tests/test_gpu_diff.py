@@ -5,7 +5,7 @@ finite differences on seeded nodes (delta h = 1e-3 m), the FP32 adjoint
 against the FP64 one, and the torch.autograd.Function.
 
 Bars: TLM vs FD <= 1e-5 relative (99% of the rays whose finite differences
-converge, and at least 70-90% of the rays converging); adjoint vs TLM <= 1e-10
+converge, 2e-5 for all; at least 60-90% of the rays converging); adjoint vs TLM <= 1e-10
 relative; adjoint vs FD <= 1e-5 relative (FP64) on every one of 64 seeded
 nodes that has a converging ray, at least 48 of them.  The map is smooth only
 inside grid cells (the cell-constant gradients jump at cell edges), so finite
@@ -61,15 +61,14 @@ def test_forward_matches_oracle_model(oracle, case):
     assert float(np.max(np.abs(e[:, ok] - o_end[:, ok]) / scale)) <= 1e-9
 
 
-# Finite differences of the oracle model, central, at two step sizes h and
-# h/2.  The model is smooth only between cell edges (its cell-constant
-# gradients jump there, so a run whose ray stage crosses an edge that the
-# other run does not measures the jump: 1e-2 and above), and each end state
-# carries rounding that the ray's own sensitivity amplifies (~45x through
-# the shoal's caustics: ~5e-10 m on x).  Two step sizes that agree to
-# CONSISTENT tell a smooth neighbourhood from a jump; the derivative is then
-# the Richardson value fd(h/2) + (fd(h/2) - fd(h)) / 3, whose eps^2 error
-# cancels.
+# Finite differences of the oracle model, central.  The model is smooth
+# only between cell edges (its cell-constant gradients jump there, so a run
+# whose ray stage crosses an edge that the other run does not measures the
+# jump: 1e-2 and above), and each end state carries rounding that the ray's
+# own sensitivity amplifies (~45x through the shoal's caustics: ~5e-10 m on
+# x).  Two step sizes that agree to CONSISTENT tell a smooth neighbourhood
+# from a jump; the derivative is then the Richardson value
+# fd(h/2) + (fd(h/2) - fd(h)) / 3, whose h^2 error cancels.
 CONSISTENT = 3e-6
 
 
@@ -82,6 +81,11 @@ def _consistent(fd1, fd2, floor):
 
 
 def test_tangent_matches_finite_differences(oracle, case):
+    # Central differences at h, h/2 and h/4 along each direction.  A ray is
+    # checked when its three differences agree pairwise and its two
+    # Richardson values (from h, h/2 and from h/2, h/4) agree to 2e-6: the
+    # finite difference is then good to about 2e-6, so the 1e-5 bar tests the
+    # tangent-linear kernel, not the differences.
     import torch
 
     from mantaray_gb300.diff import tangent
@@ -93,18 +97,19 @@ def test_tangent_matches_finite_differences(oracle, case):
     blob = np.exp(-((X - 51200.0) ** 2 + (Y - 51200.0) ** 2) / (2 * 6000.0 ** 2))
     ds0 = np.stack([rng.normal(0, 1.0, n), rng.normal(0, 1.0, n), rng.normal(0, 1e-4, n),
                     rng.normal(0, 1e-4, n)])
-    # (name, state direction, depth direction, u direction, step sizes, least
-    # share of rays whose differences converge; measured on this case: 83%,
-    # 98% and 79%).  The current's direction takes larger steps: its end-state
-    # changes are small against the rounding above.
-    cases = [("state", ds0, None, None, (1e-4, 5e-5), 0.75),
-             ("depth", np.zeros((4, n)), 50.0 * blob, None, (1e-4, 5e-5), 0.90),
-             ("u", np.zeros((4, n)), None, 0.1 * blob, (1e-3, 5e-4), 0.70)]
+    # (name, state direction, depth direction, u direction, largest step h,
+    # least share of rays checked; measured on this case: 74%, 96%, 68%).  The
+    # current's direction takes larger steps: its end-state changes are small
+    # against the rounding above.
+    cases = [("state", ds0, None, None, 1e-4, 0.65),
+             ("depth", np.zeros((4, n)), 50.0 * blob, None, 2e-4, 0.90),
+             ("u", np.zeros((4, n)), None, 0.1 * blob, 8e-4, 0.60)]
     dev = case["depth"].device
     # floors: the rounding of a difference (5e-10 m / 2 h on x and y,
     # 1.5e-16 / 2 h on kx and ky) stays below CONSISTENT times them
     floors = (1.0, 1.0, 1e-6, 1e-6)
-    for name, dst, dd, du, steps_h, least in cases:
+    fl = np.array(floors)[:, None]
+    for name, dst, dd, du, h, least in cases:
         _, d_end, st = tangent(*case["rays"], case["depth"], case["u"], case["v"], case["g"],
                                case["g"], case["dt"], case["steps"],
                                dstate0=torch.from_numpy(dst).to(dev),
@@ -113,7 +118,7 @@ def test_tangent_matches_finite_differences(oracle, case):
         d_end = d_end.cpu().numpy()
         ok = st.cpu().numpy() == 0
         fds = []
-        for eps in steps_h:
+        for eps in (h, h / 2, h / 4):
             rp = [a + eps * dst[q] for q, a in enumerate((w.x0, w.y0, w.kx0, w.ky0))]
             rm = [a - eps * dst[q] for q, a in enumerate((w.x0, w.y0, w.kx0, w.ky0))]
             ep, sp = _oracle_end(oracle, case, depth=None if dd is None else w.depth + eps * dd,
@@ -122,18 +127,18 @@ def test_tangent_matches_finite_differences(oracle, case):
                                  u=None if du is None else w.u - eps * du, rays=rm)
             ok &= (sp == 0) & (sm == 0)
             fds.append((ep - em) / (2 * eps))
+        r1, r2 = _richardson(fds[0], fds[1]), _richardson(fds[1], fds[2])
         clean = ok.copy()
         for q in range(4):
             clean &= _consistent(fds[0][q], fds[1][q], floors[q])
-        assert clean.sum() >= least * n, (name, f"{int(clean.sum())} of {n} rays converge")
-        fd = _richardson(fds[0], fds[1])
-        for q in range(4):
-            a, b = d_end[q, clean], fd[q, clean]
-            rel = np.abs(a - b) / np.maximum(np.abs(b), floors[q])
-            # <= 1e-5 for 99% of the converging rays; a ray that grazes a
-            # caustic of the shoal can sit a little above it
-            assert float(np.percentile(rel, 99)) <= 1e-5, (name, q, float(np.percentile(rel, 99)))
-            assert float(rel.max()) <= 1e-4, (name, q, float(rel.max()))
+            clean &= _consistent(fds[1][q], fds[2][q], floors[q])
+        clean &= np.all(np.abs(r1 - r2) <= 2e-6 * np.maximum(np.abs(r2), fl), axis=0)
+        assert clean.sum() >= least * n, (name, f"{int(clean.sum())} of {n} rays checked")
+        rel = np.abs(d_end[:, clean] - r2[:, clean]) / np.maximum(np.abs(r2[:, clean]), fl)
+        print(f"tangent vs finite differences, {name}: {int(clean.sum())}/{n} rays, "
+              f"p99 {np.percentile(rel, 99):.2e}, max {rel.max():.2e}")
+        assert float(np.percentile(rel, 99)) <= 1e-5, (name, float(np.percentile(rel, 99)))
+        assert float(rel.max()) <= 2e-5, (name, float(rel.max()))
 
 
 def test_adjoint_dot_product(case):
