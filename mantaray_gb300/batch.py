@@ -159,6 +159,43 @@ class BatchTracer:
         return best
 
 
+    def tune_decimation(self, x0, y0, kx0, ky0, dt, max_steps, choices, max_saved_bytes,
+                        probe_steps=None, t0=0.0, scenario=None, config=None, slowdown=1.05,
+                        repeats=2):
+        """Output decimation: the finest of `choices` (steps between stored
+        rows) whose stored rows for these rays over max_steps fit in
+        max_saved_bytes and whose probe run (`probe_steps`, default
+        min(max_steps, 1,000)) takes at most `slowdown` times the coarsest
+        fitting choice's.  Returns (decimation, {decimation: probe ms}); raises
+        ValueError when no choice fits."""
+        torch = _torch()
+        n = int(x0.numel())
+        fits = sorted(d for d in choices
+                      if d > 0 and 5 * 4 * n * (max_steps // d + 1) <= max_saved_bytes)
+        if not fits:
+            raise ValueError("no decimation in `choices` fits max_saved_bytes")
+        probe = min(max_steps, 1000) if probe_steps is None else probe_steps
+        cfg = config or default_config()
+        stream = torch.cuda.current_stream(x0.device)
+        times = {}
+        for d in fits:
+            out = self.alloc(n, probe, d, device=x0.device)
+            self.trace(x0, y0, kx0, ky0, dt, probe, t0, d, scenario, cfg, out, stream)
+            ts = []
+            for _ in range(repeats):
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                self.trace(x0, y0, kx0, ky0, dt, probe, t0, d, scenario, cfg, out, stream)
+                e1.record(stream)
+                e1.synchronize()
+                ts.append(e0.elapsed_time(e1))
+            times[d] = min(ts)
+            del out
+        limit = slowdown * times[fits[-1]]
+        return next(d for d in fits if times[d] <= limit), times
+
+
 _TUNE_CACHE: dict = {}
 
 

@@ -294,10 +294,13 @@ __device__ __forceinline__ void finish(const BatchArgs &a, RayLane &L, int statu
   L.ray = -1;
 }
 
-// The decimation as a step countdown (a ray takes fewer than 2^31 steps, so
-// a larger decimation saves no row after step 0 either way).
+// The decimation as a step countdown.  A ray takes at most max_steps <
+// 2^31 - 1 steps, so a countdown from 2^31 - 1 never reaches zero: that is
+// the period when nothing is decimated (decimation 0), and when the
+// decimation is larger (no row after step 0 either way).
 __device__ __forceinline__ int32_t save_period(const BatchArgs &a) {
-  return a.decimation > 0x7fffffff ? 0x7fffffff : static_cast<int32_t>(a.decimation);
+  return (a.decimation <= 0 || a.decimation > 0x7fffffff) ? 0x7fffffff
+                                                          : static_cast<int32_t>(a.decimation);
 }
 
 // A lane's scenario: from the kernel's parameters in the single-scenario
@@ -360,10 +363,13 @@ __device__ __forceinline__ int step_status(const ScenarioDev &s, RayLane &L, flo
 }
 
 // One RK4 step of lane L.  Returns BATCH_COMPLETE while the ray goes on.
-// The four stages run without branches between them (each stage's status is
-// a value, tested once for all four); a failed step is redone by step_status
-// for the status of its first failing stage, and the ray keeps the state it
-// had before the step.
+// The four stages run without branches between them (each stage's outcome
+// is one bit, tested once for all four); a failed step is redone by
+// step_status for the status of its first failing stage, and the ray keeps
+// the state it had before the step.  The increment k1 + 2 k2 + 2 k3 + k4 is
+// summed as the stages complete, so only the sum and the latest stage's
+// derivative stay live (register pressure, not arithmetic, bounds how many
+// warps an SM holds).
 template <int MODE>
 __device__ __forceinline__ int advance(const BatchArgs &a, RayLane &L) {
   const ScenarioDev &s = scenario<MODE>(a, L.scen);
@@ -371,24 +377,28 @@ __device__ __forceinline__ int advance(const BatchArgs &a, RayLane &L) {
   // FP64 pipe, and the compiler re-derives such values under register pressure)
   const float dt = a.dt_f;
   const float half = a.half_f;
-  float k1[4], k2[4], k3[4], k4[4];
-  const int s1 = rhs_f32<MODE, false>(s, L, L.px, L.py, L.kx, L.ky, k1);
-  const int s2 = rhs_f32<MODE, false>(s, L, fmaf(half, k1[0], L.px), fmaf(half, k1[1], L.py),
-                               fmaf(half, k1[2], L.kx), fmaf(half, k1[3], L.ky), k2);
-  const int s3 = rhs_f32<MODE, false>(s, L, fmaf(half, k2[0], L.px), fmaf(half, k2[1], L.py),
-                               fmaf(half, k2[2], L.kx), fmaf(half, k2[3], L.ky), k3);
-  const int s4 = rhs_f32<MODE, false>(s, L, fmaf(dt, k3[0], L.px), fmaf(dt, k3[1], L.py),
-                               fmaf(dt, k3[2], L.kx), fmaf(dt, k3[3], L.ky), k4);
-  if ((s1 | s2 | s3 | s4) != BATCH_COMPLETE) return step_status<MODE>(s, L, dt, half);
-  const float sixth = a.sixth_f;
+  float k[4], sum[4];
+  int fails = rhs_f32<MODE, false>(s, L, L.px, L.py, L.kx, L.ky, k);
 #pragma unroll
-  for (int q = 0; q < 4; ++q) k1[q] = sixth * fmaf(2.0f, k2[q] + k3[q], k1[q] + k4[q]);
-  kahan_add(L.px, L.cpx, k1[0]);
-  kahan_add(L.py, L.cpy, k1[1]);
-  kahan_add(L.kx, L.ckx, k1[2]);
-  kahan_add(L.ky, L.cky, k1[3]);
+  for (int q = 0; q < 4; ++q) sum[q] = k[q];
+  fails |= rhs_f32<MODE, false>(s, L, fmaf(half, k[0], L.px), fmaf(half, k[1], L.py),
+                                fmaf(half, k[2], L.kx), fmaf(half, k[3], L.ky), k);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) sum[q] = fmaf(2.0f, k[q], sum[q]);
+  fails |= rhs_f32<MODE, false>(s, L, fmaf(half, k[0], L.px), fmaf(half, k[1], L.py),
+                                fmaf(half, k[2], L.kx), fmaf(half, k[3], L.ky), k);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) sum[q] = fmaf(2.0f, k[q], sum[q]);
+  fails |= rhs_f32<MODE, false>(s, L, fmaf(dt, k[0], L.px), fmaf(dt, k[1], L.py),
+                                fmaf(dt, k[2], L.kx), fmaf(dt, k[3], L.ky), k);
+  if (fails != BATCH_COMPLETE) return step_status<MODE>(s, L, dt, half);
+  const float sixth = a.sixth_f;
+  kahan_add(L.px, L.cpx, sixth * (sum[0] + k[0]));
+  kahan_add(L.py, L.cpy, sixth * (sum[1] + k[1]));
+  kahan_add(L.kx, L.ckx, sixth * (sum[2] + k[2]));
+  kahan_add(L.ky, L.cky, sixth * (sum[3] + k[3]));
   ++L.step;
-  if (a.decimation > 0 && --L.to_save == 0) {
+  if (--L.to_save == 0) {
     L.to_save = save_period(a);
     save_row(a, L);
     ++L.saved;

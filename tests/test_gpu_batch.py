@@ -364,17 +364,26 @@ def test_edge_rays_get_their_status(mr):
 
 
 def fp64_conditioning(oracle, ob, oc, x0, y0, kx0, ky0, t0, t_end, dt, o):
-    """Per ray, the FP64 endpoint's own relative change (as endpoint_errors
-    measures it) when the ray starts 1 cm further along x; NaN where the two
-    FP64 trajectories end at different steps."""
+    """Per ray, the largest relative change of the FP64 endpoint (as
+    endpoint_errors measures it) under three start perturbations: 1 cm along
+    x, 1e-6 rad of direction, 1e-6 of relative |k|; NaN where a perturbed
+    FP64 ray ends at a different step."""
     from mantaray_gb300.batch import endpoint_errors
 
-    p = oracle.trace(ob, oc, np.asarray(x0) + 0.01, y0, kx0, ky0, t0, t_end, dt)
-    n = p[1].size
-    ii = np.arange(n)
-    last = p[1].astype(np.int64) - 1
-    last = np.where(np.all(np.isfinite(p[0][1:, last, ii]), axis=0), last, np.maximum(last - 1, 0))
-    return endpoint_errors(p[0][:, last, ii], last, o[0], o[1], per_ray=True)["rel_position"]
+    x0, y0, kx0, ky0 = (np.asarray(a, np.float64) for a in (x0, y0, kx0, ky0))
+    th, k = np.arctan2(ky0, kx0), np.hypot(kx0, ky0)
+    worst = np.zeros(x0.size)
+    for start in ((x0 + 0.01, y0, kx0, ky0),
+                  (x0, y0, k * np.cos(th + 1e-6), k * np.sin(th + 1e-6)),
+                  (x0, y0, kx0 * (1.0 + 1e-6), ky0 * (1.0 + 1e-6))):
+        p = oracle.trace(ob, oc, *start, t0, t_end, dt)
+        ii = np.arange(x0.size)
+        last = p[1].astype(np.int64) - 1
+        last = np.where(np.all(np.isfinite(p[0][1:, last, ii]), axis=0), last,
+                        np.maximum(last - 1, 0))
+        e = endpoint_errors(p[0][:, last, ii], last, o[0], o[1], per_ray=True)["rel_position"]
+        worst = np.maximum(worst, e)  # NaN stays NaN: not conditioned
+    return worst
 
 
 @pytest.mark.parametrize("size", ["fine_corner", "whole_domain"])
@@ -386,8 +395,9 @@ def test_shelf_slope_against_oracle(mr, oracle, size):
     # domain the FP64 model itself turns chaotic on the rough shelf (a 1 cm
     # start shift moves 1% of the endpoints by more than 1e-2 of their path
     # at 20,000 steps, and none by more than 3e-6 at 10,000): the bar then
-    # applies to the rays whose FP64 endpoint a 1 cm shift moves by at most
-    # 1e-4, at least 85% of them (91% measured).
+    # applies to the rays whose FP64 endpoint moves by at most 1e-4 under each
+    # of three start perturbations (1 cm in x, 1e-6 rad, 1e-6 of |k|), at
+    # least 55% of them (65% measured).
     from mantaray_gb300.batch import BatchTracer, endpoint_errors
     from mantaray_gb300.workloads import shelf_slope
 
@@ -410,7 +420,7 @@ def test_shelf_slope_against_oracle(mr, oracle, size):
     else:
         sens = fp64_conditioning(oracle, ob, oc, *rays, r["t0"], t_end, r["dt"], o)
         cond = sens <= 1e-4
-        assert cond.mean() >= 0.85, cond.mean()
+        assert cond.mean() >= 0.55, cond.mean()
         e = endpoint_errors(end[:, cond], nst[cond], o[0][:, :, cond], o[1][cond])
         check_errors(e, size)
     g = tracer.graph(*ins, r["dt"], r["steps"], t0=r["t0"])
@@ -489,3 +499,23 @@ def test_autotuner_candidates_cache_and_results(mr, tmp_path, monkeypatch):
         if x.dtype == np.float32:
             x, y = x.view(np.uint32), y.view(np.uint32)
         np.testing.assert_array_equal(x, y)
+
+
+def test_decimation_tuner_budgets(mr):
+    # The decimation tuner considers only the choices whose stored rows fit
+    # the memory budget, times each, and takes the finest one within the
+    # allowed slowdown of the coarsest.
+    from mantaray_gb300.batch import BatchTracer
+    from mantaray_gb300.workloads import seamount
+
+    w = seamount(n_rays=16384, steps=400)
+    tracer = BatchTracer([_fields(mr, w)])
+    ins = _dev(w.x0, w.y0, w.kx0, w.ky0)
+    # rows of 20 B per ray: decimation 1 -> 401 rows (131 MB), 10 -> 41, 50 -> 9, 100 -> 5
+    budget = 20 << 20
+    d, times = tracer.tune_decimation(*ins, w.dt, 400, (1, 10, 50, 100), budget, slowdown=1e9)
+    assert sorted(times) == [10, 50, 100] and d == 10
+    d, times = tracer.tune_decimation(*ins, w.dt, 400, (1, 10, 50, 100), budget, slowdown=1.0)
+    assert d in (10, 50, 100) and times[d] <= times[100]
+    with pytest.raises(ValueError):
+        tracer.tune_decimation(*ins, w.dt, 400, (1, 10), 1 << 20)
