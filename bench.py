@@ -56,7 +56,7 @@ ALG_FP32_FLOP_PER_RAY_STEP = 710.0
 # FP64 floating-point operations one ray-step executes (DADD/DMUL = 1,
 # DFMA = 2), per right-hand-side arithmetic, counted by ncu on the plain
 # kernel over the seamount workload (65,536 rays x 100 steps)
-# (sm__sass_thread_inst_executed_op_d{add,mul,fma}_pred_on; profiles/).
+# (sm__sass_thread_inst_executed_op_d{add,mul,fma}_pred_on).
 FP64_FLOP_PER_RAY_STEP = {"libm": 1401.4, "identity": 343.6}
 # FP64-pipe instructions per ray-step (sm__inst_executed_pipe_fp64 x 32, same captures)
 FP64_PIPE_INST_PER_RAY_STEP = {"libm": 945.2, "identity": 283.6}
@@ -1054,7 +1054,7 @@ def batched_arm(args, rank: int, world: int, local_rank: int):
                              "count with the current on the bathymetry's grid",
                 "executed_flop_per_ray_step": FP32_FLOP_PER_RAY_STEP,
                 "executed_frac": kernel_rate * FP32_FLOP_PER_RAY_STEP / 1e12 / fp32_peak.value}
-    # DRAM bytes per ray-step of ncu captures (profiles/), scaled to one call's ray-steps
+    # DRAM bytes per ray-step of ncu captures, scaled to one call's ray-steps
     k2_dram_per_ray_step = {"seamount": (18.60e6 / (65536 * 400),
                                          "65,536-ray x 400-step seamount capture"),
                             "shelf_slope": ((452.10e6 + 36.66e6) / 330.35e6,

@@ -19,7 +19,9 @@
 //    exp(-2kh) falls below the rounding of 1 - exp(-2kh) (kh > ~18): q then
 //    comes out 0 (or a multiple of 2^-53) instead of its true value below
 //    1e-16, so the refraction term f ~ q is off by up to that amount -- a
-//    change of k below one ulp of kx, ky per step.
+//    change of k below one ulp of kx, ky per step.  Beyond kh = 22 the
+//    values m = 1, q = 0 are taken directly (what expm1 rounds to there),
+//    without the expm1 and the reciprocal.
 // Both read the field values through the exact lookups, convert between f32
 // and f64 on the integer pipe (bits.h) and test NaN / zero on bit patterns,
 // which gives the same values as the conversion and comparison instructions.
@@ -101,11 +103,19 @@ struct RhsIdentity {
     // group_velocity's k <= 0 error (h > 0 or NaN): k is >= 0 or NaN here
     if (!(hg[0] <= 0.0f) && (__double_as_longlong(k) << 1) == 0) return RHS_ARGUMENT_OUT_OF_BOUNDS;
     const double a = k * h;
-    const double m = -expm1(-2.0 * a);              // 1 - q
-    const double q = 1.0 - m;                       // exp(-2a)
-    const double w = __drcp_rn(m * (2.0 - m));      // 1 / (m (1 + q))
-    const double r = m * w;                         // 1 / (1 + q)
-    const double th = m * r;                        // tanh a
+    double m, q, w, r, th;
+    if (a > 22.0) {
+      // deep water: exp(-2a) < 8e-20, far below half an ulp of 1, so
+      // -expm1(-2a) rounds to exactly 1 and every quantity below follows
+      // exactly: no expm1, no reciprocal
+      m = 1.0; q = 0.0; w = 1.0; r = 1.0; th = 1.0;
+    } else {
+      m = -expm1(-2.0 * a);                         // 1 - q
+      q = 1.0 - m;                                  // exp(-2a)
+      w = __drcp_rn(m * (2.0 - m));                 // 1 / (m (1 + q))
+      r = m * w;                                    // 1 / (1 + q)
+      th = m * r;                                   // tanh a
+    }
     const double gkt = (kG * k) * th;
     const double rs = rsqrt(gkt);                   // 1 / sqrt(g k tanh)
     const double q4 = 4.0 * q;
