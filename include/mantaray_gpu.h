@@ -207,6 +207,14 @@ typedef struct mr_batch_config {
   int order;           /* 1: sort the rays by starting cell and direction before
                           tracing, so a warp's rays share cell records (results
                           per ray are unchanged); 0: trace in index order */
+  int tile;            /* 1: each warp keeps an 8 x 8-cell tile of the cell
+                          records in shared memory, loaded by the tensor memory
+                          accelerator and moved to where most of its rays are;
+                          a ray entering a cell of the tile reads it there
+                          (results per ray are unchanged).  One scenario with
+                          its current gridded on the bathymetry's grid only
+                          (MR_ERR_INVALID_ARGUMENT otherwise); 0: cell records
+                          from global memory */
 } mr_batch_config;
 
 /* Per-ray status of the batched form. */

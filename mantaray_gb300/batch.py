@@ -33,8 +33,8 @@ def default_config() -> N.BatchConfig:
 
 
 def make_config(block=128, blocks_per_sm=4, rays_per_lane=1, rebase_interval=32,
-                order=0) -> N.BatchConfig:
-    return N.BatchConfig(block, blocks_per_sm, rays_per_lane, rebase_interval, order)
+                order=0, tile=0) -> N.BatchConfig:
+    return N.BatchConfig(block, blocks_per_sm, rays_per_lane, rebase_interval, order, tile)
 
 
 @dataclass
@@ -62,6 +62,24 @@ class BatchTracer:
         N.check(L.mr_batch_create(n, bs, cs, ctypes.byref(out)))
         self._h = out
         self.n_scenarios = n
+        self._tiles = None
+
+    @property
+    def tiles_supported(self) -> bool:
+        """Whether mr_batch_config.tile = 1 is accepted: one scenario with its
+        current gridded on the bathymetry's grid (tried once with a call of
+        no rays, which checks the configuration and traces nothing)."""
+        if self._tiles is None:
+            torch = _torch()
+            z = torch.empty(0, dtype=torch.float64, device="cuda")
+            out = self.alloc(0, 1, 0, device="cuda")
+            rc = N.load().mr_batch_trace_device(
+                self._h, 0, None, z.data_ptr(), z.data_ptr(), z.data_ptr(), z.data_ptr(), 0.0,
+                1.0, 1, 0, 0, None, out.end_state.data_ptr(), out.n_steps.data_ptr(),
+                out.n_saved.data_ptr(), out.status.data_ptr(),
+                ctypes.byref(make_config(128, 4, 1, 32, 0, 1)), None)
+            self._tiles = rc == N.OK
+        return self._tiles
 
     def close(self):
         if self._h and self._h.value:
@@ -133,6 +151,11 @@ class BatchTracer:
                                                                       (2, 4, 6, 8, 12),
                                                                       (1, 2), (0, 1))
                           if b * bps <= 2048]
+            if self.tiles_supported:
+                # shared-memory tiles of cell records (one ray per lane, ordered rays)
+                candidates += [make_config(b, bps, 1, 32, 1, 1)
+                               for b, bps in itertools.product((64, 128, 256), (2, 4, 6, 8, 12))
+                               if b * bps <= 2048]
         out = self.alloc(int(x0.numel()), probe_steps, 0, device=x0.device)
         best, best_t = None, float("inf")
         stream = torch.cuda.current_stream(x0.device)

@@ -19,6 +19,7 @@
 // same equations as the plain form, in single precision.
 #pragma once
 
+#include <cuda.h>
 #include <stdint.h>
 
 namespace mr {
@@ -49,7 +50,18 @@ enum BatchStatus : uint8_t {
   BATCH_BAD_WAVENUMBER = 3,// k <= 0 or non-finite state
 };
 
+// Shared-memory tile of one warp (the tile build): kTileCells x kTileCells
+// cells of both fields' records, bathymetry first.
+constexpr int kTileCells = 8;
+constexpr int kTileBathyBytes = kTileCells * kTileCells * 2 * 16;
+constexpr int kTileBytes = kTileCells * kTileCells * 5 * 16;
+
 struct BatchArgs {
+  // tensor maps of scenario 0's cell records (the tile build): bathymetry
+  // [ny-1][nx-1][8 floats], current [ny-1][nx-1][12 floats]
+  CUtensorMap tmap_bathy;
+  CUtensorMap tmap_current;
+  int tile;                  // 1: the tile build
   const ScenarioDev *scen;   // [n_scenarios]
   ScenarioDev scen0;         // scen[0] by value: the single-scenario build reads it from
                              // the kernel's parameters, with no load

@@ -2,6 +2,7 @@
 // scenario packing, device-buffer tracing, and CUDA-graph replay.
 
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 #include <math.h>
 #include <string.h>
 
@@ -107,6 +108,37 @@ int pack_current(mr_batch *b, const mr_current *c, mr::PackedGrid *g, cudaStream
   return MR_OK;
 }
 
+// A tensor map of a packed cell array (ny-1 rows of nx-1 cells of
+// `floats` FP32 values) with boxes of kTileCells x kTileCells cells, for the
+// tile build's copies.  cuTensorMapEncodeTiled comes from the driver through
+// the runtime's entry-point query (the library links no driver library).
+int encode_cells(CUtensorMap *m, const float4 *cells, int nx, int ny, int floats) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = [] {
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault,
+                                         &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      (void)cudaGetLastError();
+      fn = nullptr;
+    }
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }();
+  if (!encode) return fail(MR_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+  const cuuint64_t dims[3] = {static_cast<cuuint64_t>(floats), static_cast<cuuint64_t>(nx - 1),
+                              static_cast<cuuint64_t>(ny - 1)};
+  const cuuint64_t strides[2] = {static_cast<cuuint64_t>(floats) * 4,
+                                 static_cast<cuuint64_t>(nx - 1) * floats * 4};
+  const cuuint32_t box[3] = {static_cast<cuuint32_t>(floats), mr::kTileCells, mr::kTileCells};
+  const cuuint32_t step[3] = {1, 1, 1};
+  const CUresult r = encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
+                            const_cast<float4 *>(cells), dims, strides, box, step,
+                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(MR_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", int(r));
+  return MR_OK;
+}
+
 void order_free(mr_order_buffers *o) {
   if (o->mem) cudaFree(o->mem);
   *o = mr_order_buffers();
@@ -164,6 +196,10 @@ int check_config(const mr_batch_config *cfg) {
     return fail(MR_ERR_INVALID_ARGUMENT, "rebase_interval must be >= 1");
   if (cfg->order != 0 && cfg->order != 1)
     return fail(MR_ERR_INVALID_ARGUMENT, "order must be 0 or 1");
+  if (cfg->tile != 0 && cfg->tile != 1)
+    return fail(MR_ERR_INVALID_ARGUMENT, "tile must be 0 or 1");
+  if (cfg->tile && cfg->rays_per_lane != 1)
+    return fail(MR_ERR_INVALID_ARGUMENT, "tile staging traces one ray per lane");
   return MR_OK;
 }
 
@@ -206,6 +242,15 @@ int fill_args(mr_batch *b, size_t n, size_t n_stride, const uint8_t *ray_scenari
                   static_cast<long long>(max_steps / decimation + 1));
   }
   if (!(dt > 0.0) || !isfinite(t0)) return fail(MR_ERR_INVALID_ARGUMENT, "dt must be > 0");
+  if (cfg->tile && !b->has_tmaps)
+    return fail(MR_ERR_INVALID_ARGUMENT,
+                "tile staging needs one scenario with its current gridded on the bathymetry's "
+                "grid");
+  a->tile = cfg->tile;
+  if (b->has_tmaps) {
+    a->tmap_bathy = b->tmap_bathy;
+    a->tmap_current = b->tmap_current;
+  }
   a->scen = b->scen;
   a->scen0 = b->host_scen[0];
   a->all_same_grid = all_same_grid(b);
@@ -283,6 +328,7 @@ int mr_batch_default_config(mr_batch_config *cfg) {
   cfg->rays_per_lane = 1;
   cfg->rebase_interval = 32;
   cfg->order = 0;
+  cfg->tile = 0;
   return MR_OK;
 }
 
@@ -336,6 +382,15 @@ int mr_batch_create(size_t n_scenarios, const mr_bathymetry *const *bathy,
     while ((1 << sbits) < b->n_scenarios) ++sbits;
     b->order_scen_shift = 8 + 2 * cbits;
     b->order_passes = (b->order_scen_shift + sbits + 7) / 8;
+  }
+  if (rc == MR_OK && e == cudaSuccess && n_scenarios == 1 && b->host_scen[0].same_grid) {
+    const mr::ScenarioDev &sc = b->host_scen[0];
+    rc = encode_cells(&b->tmap_bathy, sc.bathy.cells, sc.bathy.nx, sc.bathy.ny, 8);
+    if (rc == MR_OK)
+      rc = encode_cells(&b->tmap_current, sc.current.cells, sc.current.nx, sc.current.ny, 12);
+    // without the driver's encoder the batch still traces, without tiles
+    if (rc != MR_OK) rc = MR_OK;
+    else b->has_tmaps = true;
   }
   if (rc == MR_OK && e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (rc == MR_OK && e != cudaSuccess) rc = cuda_fail(e, "building the batched scenarios");
@@ -410,7 +465,7 @@ int mr_batch_graph_create(mr_batch *b, size_t n_max, const uint8_t *ray_scenario
   // the integrator build for this shape, chosen (an occupancy query) before
   // the capture begins
   (void)mr::rk4_f32_function(cfg->rays_per_lane, cfg->block, cfg->blocks_per_sm,
-                             b->n_scenarios, all_same_grid(b));
+                             b->n_scenarios, all_same_grid(b), cfg->tile);
   if (e == cudaSuccess) e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
     cudaError_t le = enqueue(b, a, cfg, &gr->ord, s);
@@ -434,7 +489,7 @@ int mr_batch_graph_create(mr_batch *b, size_t n_max, const uint8_t *ray_scenario
         gr->order_params = p;
       } else if (p.func == mr::rk4_f32_function(cfg->rays_per_lane, cfg->block,
                                                 cfg->blocks_per_sm, b->n_scenarios,
-                                                all_same_grid(b))) {
+                                                all_same_grid(b), cfg->tile)) {
         gr->kernel_node = nodes[i];
         gr->params = p;
       }

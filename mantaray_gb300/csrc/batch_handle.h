@@ -30,6 +30,11 @@ struct mr_batch {
   mr_order_buffers ord;              // ordering scratch of direct calls, grown on demand
   int order_scen_shift = 8;          // key layout of the ordering (order.cu)
   int order_passes = 1;
+  // tensor maps of the cell records for the tile build (one scenario with its
+  // current on the bathymetry's grid), made at creation
+  CUtensorMap tmap_bathy{};
+  CUtensorMap tmap_current{};
+  bool has_tmaps = false;
 };
 
 // 1 when every scenario's current is gridded on its bathymetry's grid (the

@@ -94,19 +94,27 @@ __device__ __forceinline__ GridPos grid_pos(const PackedGrid &g, double ox, doub
 // meaningless.  The cell's coordinates are integral floats (exact sums),
 // tested against the grid's bounds.  Cells are indexed in 32 bits (the
 // batch refuses grids of 2^31 cells or more).
+// ix, iy: the cell's column and row (meaningful when inside).
 __device__ __forceinline__ bool locate(const PackedGrid &g, const GridPos &p, float px, float py,
-                                       int *cell, float *fx, float *fy) {
+                                       int *cell, float *fx, float *fy, int *ix, int *iy) {
   const float ux = fmaf(px, g.inv_sp_x, p.f0);
   const float uy = fmaf(py, g.inv_sp_y, p.g0);
   const float flx = floorf(ux), fly = floorf(uy);
   const float cx = p.fi0 + flx, cy = p.fj0 + fly;
   // saturating conversions and unsigned arithmetic: defined for any position
-  *cell = static_cast<int>(static_cast<unsigned>(__float2int_rz(cy)) *
-                               static_cast<unsigned>(g.nx - 1) +
-                           static_cast<unsigned>(__float2int_rz(cx)));
+  *ix = __float2int_rz(cx);
+  *iy = __float2int_rz(cy);
+  *cell = static_cast<int>(static_cast<unsigned>(*iy) * static_cast<unsigned>(g.nx - 1) +
+                           static_cast<unsigned>(*ix));
   *fx = ux - flx;
   *fy = uy - fly;
   return cx >= 0.0f && cx <= g.cx_max && cy >= 0.0f && cy <= g.cy_max;
+}
+
+__device__ __forceinline__ bool locate(const PackedGrid &g, const GridPos &p, float px, float py,
+                                       int *cell, float *fx, float *fy) {
+  int ix, iy;
+  return locate(g, p, px, py, cell, fx, fy, &ix, &iy);
 }
 
 // c = the cell's bilinear coefficients (batch.h): c.x + c.y fx + c.z fy +
@@ -205,6 +213,145 @@ __device__ __forceinline__ void load_same_grid_cell(const ScenarioDev &s, CellCa
   }
 }
 
+// ---------------------------------------------------- shared-memory tiles --
+// The tile build (mode 2, BatchArgs::tile): each warp holds kTileCells^2
+// cells of both fields' records in shared memory, a box of the cell arrays
+// that the tensor memory accelerator copies in (one cp.async.bulk.tensor per
+// field, completion counted on the warp's mbarrier).  A lane entering a cell
+// of the tile reads its records there instead of from global memory; the
+// values are the same, so results are bit-identical to the build without
+// tiles.  Every 4 steps the warp moves its tile onto an outside lane's cell
+// when most of its live lanes are outside it.  Waits are bounded: a copy
+// that does not complete within kTileWaitPolls polls turns the warp's tiles
+// off for the rest of the launch (global memory serves every lane).
+
+constexpr int kTileWaitPolls = 1 << 22;
+
+struct WarpTile {
+  int ti, tj;          // tile origin (cell column and row)
+  bool valid;          // the tile holds those cells
+  bool off;            // tiles turned off (a copy timed out)
+  bool pending;        // a timed-out copy may still be in flight
+  uint32_t phase;      // parity of the mbarrier phase the next copy completes
+  uint32_t smem;       // shared-memory address of this warp's tile
+  uint32_t mbar;       // shared-memory address of this warp's mbarrier
+  const float4 *tb;    // the tile's bathymetry records (then the current's)
+};
+
+extern __shared__ __align__(128) unsigned char k2_tile_smem[];
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t mbar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n"
+      " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(mbar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t mbar, uint32_t parity) {
+  for (int i = 0; i < kTileWaitPolls; ++i)
+    if (mbar_try_wait(mbar, parity)) return true;
+  return false;
+}
+
+// The warp's tile and mbarrier (lane 0 initialises the barrier: one arrival
+// per phase, lane 0's, plus the copies' byte count).
+__device__ __forceinline__ WarpTile tile_init() {
+  WarpTile W;
+  const int warp = threadIdx.x >> 5;
+  const int warps = blockDim.x >> 5;
+  W.smem = static_cast<uint32_t>(__cvta_generic_to_shared(k2_tile_smem)) + warp * kTileBytes;
+  W.mbar = static_cast<uint32_t>(__cvta_generic_to_shared(k2_tile_smem)) + warps * kTileBytes +
+           warp * 8;
+  W.tb = reinterpret_cast<const float4 *>(k2_tile_smem + warp * kTileBytes);
+  W.ti = W.tj = 0;
+  W.valid = W.off = W.pending = false;
+  W.phase = 0;
+  if ((threadIdx.x & 31) == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(W.mbar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncwarp();
+  return W;
+}
+
+// Copies the tile with origin (ti, tj) in, waits for it (bounded).  Called by
+// the whole warp at the same point; the warp's earlier reads of the old tile
+// are complete (ordered before the copy by __syncwarp and the proxy fence).
+__device__ __forceinline__ void tile_load(const BatchArgs &a, WarpTile &W, int ti, int tj) {
+  __syncwarp();
+  if ((threadIdx.x & 31) == 0) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(W.mbar),
+                 "r"(kTileBytes)
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(W.smem),
+        "l"(reinterpret_cast<uint64_t>(&a.tmap_bathy)), "r"(0), "r"(ti), "r"(tj), "r"(W.mbar)
+        : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(W.smem + kTileBathyBytes),
+        "l"(reinterpret_cast<uint64_t>(&a.tmap_current)), "r"(0), "r"(ti), "r"(tj),
+        "r"(W.mbar)
+        : "memory");
+  }
+  const bool done = __all_sync(kFull, mbar_wait_bounded(W.mbar, W.phase));
+  W.phase ^= 1u;
+  if (done) {
+    W.ti = ti;
+    W.tj = tj;
+    W.valid = true;
+  } else {
+    W.valid = false;
+    W.off = true;
+    W.pending = true;
+  }
+}
+
+// Before the warp exits: a copy that timed out gets one more bounded wait,
+// so that none lands in shared memory after the block has left.
+__device__ __forceinline__ void tile_finish(const WarpTile &W) {
+  if (W.pending) (void)mbar_wait_bounded(W.mbar, W.phase ^ 1u);
+}
+
+// The records of cell cb (column ix, row iy) of both fields, mode 2, unless
+// the lane holds them: from the warp's tile when the cell is in it.
+__device__ __forceinline__ void load_same_grid_cell_tile(const ScenarioDev &s, CellCache &C,
+                                                         const WarpTile &W, int cb, int ix,
+                                                         int iy) {
+  if (cb != C.bkey) {
+    const unsigned dx = static_cast<unsigned>(ix - W.ti), dy = static_cast<unsigned>(iy - W.tj);
+    if (W.valid && dx < static_cast<unsigned>(kTileCells) &&
+        dy < static_cast<unsigned>(kTileCells)) {
+      const int c = static_cast<int>(dy) * kTileCells + static_cast<int>(dx);
+      const float4 *tb = W.tb;
+      const float4 *tc = tb + kTileCells * kTileCells * 2;
+      C.b0 = tb[2 * c];
+      const float4 b1 = tb[2 * c + 1];
+      C.bx = b1.x;
+      C.by = b1.y;
+      C.c0 = tc[3 * c];
+      C.c1 = tc[3 * c + 1];
+      C.c2 = tc[3 * c + 2];
+    } else {
+      C.b0 = __ldg(s.bathy.cells + static_cast<int64_t>(cb) * 2);
+      const float4 b1 = __ldg(s.bathy.cells + static_cast<int64_t>(cb) * 2 + 1);
+      C.bx = b1.x;
+      C.by = b1.y;
+      C.c0 = __ldg(s.current.cells + static_cast<int64_t>(cb) * 3);
+      C.c1 = __ldg(s.current.cells + static_cast<int64_t>(cb) * 3 + 1);
+      C.c2 = __ldg(s.current.cells + static_cast<int64_t>(cb) * 3 + 2);
+    }
+    C.bkey = cb;
+  }
+}
+
 // One right-hand side in FP32 at offset (px, py), wavenumber (kx, ky).
 // The fields come from the lane's cell records (loaded when the lane does not
 // hold the cell; a point outside a grid loads nothing and uses the records
@@ -215,17 +362,21 @@ __device__ __forceinline__ void load_same_grid_cell(const ScenarioDev &s, CellCa
 // meaningful only when complete.  Written without early returns so that the
 // four stages of a step run with no branch between them.  MODE 2 and 3: the
 // current is gridded on the bathymetry's grid, so one cell (one key, one
-// test) serves both fields.
-template <int MODE, bool EXACT>
-__device__ __forceinline__ int rhs_f32(const ScenarioDev &s, RayLane &L, float px, float py,
-                                       float kx, float ky, float d[4]) {
+// test) serves both fields.  TILE (mode 2): records from the warp's tile
+// when the cell is in it.
+template <int MODE, bool EXACT, bool TILE>
+__device__ __forceinline__ int rhs_f32(const ScenarioDev &s, RayLane &L, const WarpTile &W,
+                                       float px, float py, float kx, float ky, float d[4]) {
   CellCache &C = L.cache;
-  int cb;
+  int cb, ix, iy;
   float fx, fy;
-  bool inside = locate(s.bathy, L.pb, px, py, &cb, &fx, &fy);
+  bool inside = locate(s.bathy, L.pb, px, py, &cb, &fx, &fy, &ix, &iy);
   float u, v, dudx, dudy, dvdx, dvdy;
   if (MODE == 2 || MODE == 3) {
-    load_same_grid_cell(s, C, inside ? cb : C.bkey);
+    if (TILE)
+      load_same_grid_cell_tile(s, C, W, inside ? cb : C.bkey, ix, iy);
+    else
+      load_same_grid_cell(s, C, inside ? cb : C.bkey);
     u = bilin(C.c0, fx, fy);
     v = bilin(C.c1, fx, fy);
     dudx = C.c2.x; dudy = C.c2.y; dvdx = C.c2.z; dvdy = C.c2.w;
@@ -343,13 +494,13 @@ __device__ __forceinline__ void start(const BatchArgs &a, RayLane &L, int64_t r)
 // again, in order, up to the first that fails (the same arithmetic on the
 // same inputs, so the same values and the same first failure).  Taken once
 // per ray at most: the ray ends there.  One stage in a loop: little code.
-template <int MODE>
-__device__ __forceinline__ int step_status(const ScenarioDev &s, RayLane &L, float dt,
-                                           float half) {
+template <int MODE, bool TILE>
+__device__ __forceinline__ int step_status(const ScenarioDev &s, RayLane &L, const WarpTile &W,
+                                           float dt, float half) {
   float k[4], x[4] = {L.px, L.py, L.kx, L.ky};
 #pragma unroll 1
   for (int st = 0; st < 4; ++st) {
-    const int r = rhs_f32<MODE, true>(s, L, x[0], x[1], x[2], x[3], k);
+    const int r = rhs_f32<MODE, true, TILE>(s, L, W, x[0], x[1], x[2], x[3], k);
     if (r != BATCH_COMPLETE) return r;
     const float w = st == 2 ? dt : half;
     x[0] = fmaf(w, k[0], L.px);
@@ -370,28 +521,28 @@ __device__ __forceinline__ int step_status(const ScenarioDev &s, RayLane &L, flo
 // summed as the stages complete, so only the sum and the latest stage's
 // derivative stay live (register pressure, not arithmetic, bounds how many
 // warps an SM holds).
-template <int MODE>
-__device__ __forceinline__ int advance(const BatchArgs &a, RayLane &L) {
+template <int MODE, bool TILE>
+__device__ __forceinline__ int advance(const BatchArgs &a, RayLane &L, const WarpTile &W) {
   const ScenarioDev &s = scenario<MODE>(a, L.scen);
   // step constants in FP32 from the host (a conversion here would run on the
   // FP64 pipe, and the compiler re-derives such values under register pressure)
   const float dt = a.dt_f;
   const float half = a.half_f;
   float k[4], sum[4];
-  int fails = rhs_f32<MODE, false>(s, L, L.px, L.py, L.kx, L.ky, k);
+  int fails = rhs_f32<MODE, false, TILE>(s, L, W, L.px, L.py, L.kx, L.ky, k);
 #pragma unroll
   for (int q = 0; q < 4; ++q) sum[q] = k[q];
-  fails |= rhs_f32<MODE, false>(s, L, fmaf(half, k[0], L.px), fmaf(half, k[1], L.py),
+  fails |= rhs_f32<MODE, false, TILE>(s, L, W, fmaf(half, k[0], L.px), fmaf(half, k[1], L.py),
                                 fmaf(half, k[2], L.kx), fmaf(half, k[3], L.ky), k);
 #pragma unroll
   for (int q = 0; q < 4; ++q) sum[q] = fmaf(2.0f, k[q], sum[q]);
-  fails |= rhs_f32<MODE, false>(s, L, fmaf(half, k[0], L.px), fmaf(half, k[1], L.py),
+  fails |= rhs_f32<MODE, false, TILE>(s, L, W, fmaf(half, k[0], L.px), fmaf(half, k[1], L.py),
                                 fmaf(half, k[2], L.kx), fmaf(half, k[3], L.ky), k);
 #pragma unroll
   for (int q = 0; q < 4; ++q) sum[q] = fmaf(2.0f, k[q], sum[q]);
-  fails |= rhs_f32<MODE, false>(s, L, fmaf(dt, k[0], L.px), fmaf(dt, k[1], L.py),
+  fails |= rhs_f32<MODE, false, TILE>(s, L, W, fmaf(dt, k[0], L.px), fmaf(dt, k[1], L.py),
                                 fmaf(dt, k[2], L.kx), fmaf(dt, k[3], L.ky), k);
-  if (fails != BATCH_COMPLETE) return step_status<MODE>(s, L, dt, half);
+  if (fails != BATCH_COMPLETE) return step_status<MODE, TILE>(s, L, W, dt, half);
   const float sixth = a.sixth_f;
   kahan_add(L.px, L.cpx, sixth * (sum[0] + k[0]));
   kahan_add(L.py, L.cpy, sixth * (sum[1] + k[1]));
@@ -410,7 +561,27 @@ __device__ __forceinline__ int advance(const BatchArgs &a, RayLane &L) {
   return BATCH_COMPLETE;
 }
 
-template <int RPT, int MODE>
+// The tile build's upkeep, every 4 steps: when most of the warp's live
+// lanes are in cells outside its tile, the tile moves so that the first such
+// lane's cell sits at its centre.
+template <int MODE>
+__device__ __forceinline__ void tile_refresh(const BatchArgs &a, const RayLane &L, WarpTile &W) {
+  const ScenarioDev &s = scenario<MODE>(a, L.scen);
+  int cb = 0, ix = 0, iy = 0;
+  float fx, fy;
+  const bool in_grid = L.ray >= 0 && locate(s.bathy, L.pb, L.px, L.py, &cb, &fx, &fy, &ix, &iy);
+  const bool in_tile = W.valid && static_cast<unsigned>(ix - W.ti) < kTileCells &&
+                       static_cast<unsigned>(iy - W.tj) < kTileCells;
+  const unsigned live = __ballot_sync(kFull, in_grid);
+  const unsigned out = __ballot_sync(kFull, in_grid && !in_tile);
+  if (W.off || 2 * __popc(out) <= __popc(live)) return;
+  const int src = __ffs(out) - 1;
+  const int ti = __shfl_sync(kFull, ix, src) - kTileCells / 2;
+  const int tj = __shfl_sync(kFull, iy, src) - kTileCells / 2;
+  tile_load(a, W, ti, tj);
+}
+
+template <int RPT, int MODE, bool TILE>
 __device__ __forceinline__ void k2_body(const BatchArgs &a) {
   const int lane = threadIdx.x & 31;
   const unsigned lt_mask = (1u << lane) - 1u;
@@ -419,6 +590,9 @@ __device__ __forceinline__ void k2_body(const BatchArgs &a) {
   RayLane L[RPT];
 #pragma unroll
   for (int j = 0; j < RPT; ++j) L[j].ray = -1;
+  WarpTile W;
+  if (TILE) W = tile_init();
+  int iter = 0;
   while (true) {
     // refill empty slots from the work queue, one atomic per warp and slot
 #pragma unroll
@@ -440,6 +614,7 @@ __device__ __forceinline__ void k2_body(const BatchArgs &a) {
 #pragma unroll
     for (int j = 0; j < RPT; ++j) live |= L[j].ray >= 0;
     if (!__any_sync(kFull, live)) break;
+    if (TILE && (iter++ & 3) == 0) tile_refresh<MODE>(a, L[0], W);
 #pragma unroll
     for (int j = 0; j < RPT; ++j) {
       if (L[j].ray < 0) continue;
@@ -447,10 +622,11 @@ __device__ __forceinline__ void k2_body(const BatchArgs &a) {
         finish(a, L[j], BATCH_COMPLETE);
         continue;
       }
-      const int st = advance<MODE>(a, L[j]);
+      const int st = advance<MODE, TILE>(a, L[j], W);
       if (st != BATCH_COMPLETE) finish(a, L[j], st);
     }
   }
+  if (TILE) tile_finish(W);
 }
 
 // One ray per lane, two builds.  rk4_f32_kernel_1 takes the compiler's
@@ -470,12 +646,21 @@ __device__ __forceinline__ void k2_body(const BatchArgs &a) {
 // lookup); 2 is mode 1 and 3 is mode 0 with the current gridded on the
 // bathymetry's grid (every scenario's, for 3).
 template <int MODE>
-__global__ void __launch_bounds__(256) rk4_f32_kernel_1(BatchArgs a) { k2_body<1, MODE>(a); }
+__global__ void __launch_bounds__(256) rk4_f32_kernel_1(BatchArgs a) { k2_body<1, MODE, false>(a); }
 template <int MODE>
-__global__ void __maxnreg__(72) rk4_f32_kernel_1r(BatchArgs a) { k2_body<1, MODE>(a); }
+__global__ void __maxnreg__(72) rk4_f32_kernel_1r(BatchArgs a) { k2_body<1, MODE, false>(a); }
 // Two rays per lane hold twice the lane state: no cap.
 template <int MODE>
-__global__ void __launch_bounds__(256) rk4_f32_kernel_2(BatchArgs a) { k2_body<2, MODE>(a); }
+__global__ void __launch_bounds__(256) rk4_f32_kernel_2(BatchArgs a) { k2_body<2, MODE, false>(a); }
+// The tile build (mode 2): one ray per lane (the compiler's register count,
+// 80; capped at 72 it spilled), each warp's tile in dynamic
+// shared memory (kTileBytes per warp, then 8 bytes of mbarrier per warp); the
+// arguments stay in the parameter space (__grid_constant__) because the
+// copies read the tensor maps from there.
+template <int MODE>
+__global__ void __launch_bounds__(256) rk4_f32_kernel_1t(const __grid_constant__ BatchArgs a) {
+  k2_body<1, MODE, true>(a);
+}
 
 }  // namespace
 

@@ -162,9 +162,14 @@ static const void *table_builds[2][3] = {
 // size (multiples of 32 up to 256), queried once; 0: not yet known.
 static std::atomic<int> g_resident_1[4][9];
 
+size_t rk4_f32_tile_smem(int block) {
+  return static_cast<size_t>(block / 32) * (kTileBytes + 8);
+}
+
 const void *rk4_f32_function(int rays_per_lane, int block, int blocks_per_sm, int n_scenarios,
-                             int same_grid) {
+                             int same_grid, int tile) {
   const int mode = n_scenarios == 1 ? (same_grid ? 2 : 1) : (same_grid ? 3 : 0);
+  if (tile) return (mode == 2 && rays_per_lane == 1) ? rk4_f32_one_function(3, 1) : nullptr;
   const void *fn[3];
   for (int k = 0; k < 3; ++k)
     fn[k] = (mode == 1 || mode == 2) ? rk4_f32_one_function(k, mode == 2)
@@ -194,9 +199,11 @@ cudaError_t launch_rk4_f32(const BatchArgs &a, int block, int blocks_per_sm, int
   if (e != cudaSuccess) return e;
   const unsigned grid = static_cast<unsigned>(sms * blocks_per_sm);
   void *args[] = {const_cast<BatchArgs *>(&a)};
-  return cudaLaunchKernel(rk4_f32_function(rays_per_lane, block, blocks_per_sm, a.n_scenarios,
-                                           a.all_same_grid),
-                          dim3(grid), dim3(block), args, 0, stream);
+  const void *fn = rk4_f32_function(rays_per_lane, block, blocks_per_sm, a.n_scenarios,
+                                    a.all_same_grid, a.tile);
+  if (!fn) return cudaErrorInvalidValue;
+  return cudaLaunchKernel(fn, dim3(grid), dim3(block), args, a.tile ? rk4_f32_tile_smem(block) : 0,
+                          stream);
 }
 
 }  // namespace mr

@@ -519,3 +519,60 @@ def test_decimation_tuner_budgets(mr):
     assert d in (10, 50, 100) and times[d] <= times[100]
     with pytest.raises(ValueError):
         tracer.tune_decimation(*ins, w.dt, 400, (1, 10), 1 << 20)
+
+
+@pytest.mark.parametrize("field", ["seamount", "shelf_slope"])
+def test_tiles_give_identical_results(mr, field):
+    # Shared-memory tiles of the cell records (copied in by the tensor memory
+    # accelerator) change where a lane reads a cell's records, not their
+    # values: every output bit equals the untiled build's, for several launch
+    # shapes and through a captured graph.
+    from mantaray_gb300.batch import BatchTracer, make_config
+    from mantaray_gb300.workloads import seamount, shelf_slope
+
+    if field == "seamount":
+        w = seamount(n_rays=8192, steps=600)
+        b, c = _fields(mr, w)
+        rays, dt, steps = (w.x0, w.y0, w.kx0, w.ky0), w.dt, 600
+    else:
+        f, r = shelf_slope(n=2048, n_rays=8192, steps=2000)
+        b = mr.Bathymetry.grid(f[0], f[1], f[2])
+        c = mr.Current.grid(f[3], f[4], f[5], f[6])
+        rays, dt, steps = (r["x0"], r["y0"], r["kx0"], r["ky0"]), r["dt"], 2000
+    tracer = BatchTracer([(b, c)])
+    assert tracer.tiles_supported
+    ins = _dev(*rays)
+
+    def bits(o):
+        return [o.end_state.cpu().numpy().view(np.uint64), o.n_steps.cpu().numpy(),
+                o.status.cpu().numpy(), o.saved.cpu().numpy().view(np.uint32)]
+
+    ref = bits(tracer.trace(*ins, dt, steps, decimation=50, config=make_config(128, 4, 1, 32, 1)))
+    for shape in ((128, 4, 1, 32, 1, 1), (64, 8, 1, 32, 1, 1), (256, 2, 1, 32, 0, 1)):
+        got = bits(tracer.trace(*ins, dt, steps, decimation=50, config=make_config(*shape)))
+        for x, y in zip(got, ref):
+            np.testing.assert_array_equal(x, y)
+    g = tracer.graph(*ins, dt, steps, decimation=50, config=make_config(128, 6, 1, 32, 1, 1))
+    g.launch()
+    for x, y in zip(bits(g.out), ref):
+        np.testing.assert_array_equal(x, y)
+    g.close()
+
+
+def test_tiles_refused_where_they_do_not_apply(mr):
+    from mantaray_gb300 import MantarayError
+    from mantaray_gb300.batch import BatchTracer, make_config
+
+    x = np.arange(40, dtype=np.float32) * 100.0
+    xd = x.astype(np.float64)
+    b = mr.Bathymetry.grid(x, x, np.full(1600, 500.0))
+    c = mr.Current.grid(xd, xd, np.zeros(1600), np.zeros(1600))
+    ins = _dev(np.full(64, 1000.0), np.full(64, 1500.0), np.full(64, 0.03), np.zeros(64))
+    two = BatchTracer([(b, c), (b, c)])  # two scenarios
+    own = BatchTracer([(b, mr.Current.constant(0.1, 0.0))])  # current not on the grid
+    for tr in (two, own):
+        assert not tr.tiles_supported
+        with pytest.raises(MantarayError, match="tile staging"):
+            tr.trace(*ins, 1.0, 10, config=make_config(128, 4, 1, 32, 0, 1))
+    with pytest.raises(MantarayError, match="one ray per lane"):
+        BatchTracer([(b, c)]).trace(*ins, 1.0, 10, config=make_config(128, 4, 2, 32, 0, 1))
