@@ -102,7 +102,7 @@ def parse():
     p.add_argument("--no-autotune", action="store_true")
     p.add_argument("--launch", default=None,
                    help="batched form: fixed launch shape 'block,blocks_per_sm,rays_per_lane,"
-                        "order' instead of the autotuner's")
+                        "order[,tile]' instead of the autotuner's")
     # the target measurements reported beside the plain form's line
     p.add_argument("--no-north-star", action="store_true",
                    help="plain form: skip the shelf-slope batched-vs-plain and adjoint-vs-"
@@ -598,7 +598,7 @@ def north_star_batched(args, dev, stream, flush) -> dict:
 
     import mantaray_gb300 as mr
     from mantaray_gb300 import workloads as W
-    from mantaray_gb300.batch import BatchTracer
+    from mantaray_gb300.batch import BatchTracer, make_config
 
     nominal = args.ns_rays
     cap = nominal * 3 // 2
@@ -614,8 +614,12 @@ def north_star_batched(args, dev, stream, flush) -> dict:
     name = (f"shelf_slope_{nominal}rays_pm50pct_{args.ns_grid}x{args.ns_grid}_dt2_"
             f"{steps}steps_graph_replay")
     probe = min(cap, 1 << 20)
-    cfg = tracer.autotune(*[t[:probe] for t in ins], dt, min(steps, 1000), t0=t0,
-                          cache_key=f"{torch.cuda.get_device_name(dev)}:{name}:{probe}")
+    if args.launch:
+        blk, bps, rpl, order, *tile = (int(v) for v in args.launch.split(","))
+        cfg = make_config(blk, bps, rpl, 32, order, tile[0] if tile else 0)
+    else:
+        cfg = tracer.autotune(*[t[:probe] for t in ins], dt, min(steps, 1000), t0=t0,
+                              cache_key=f"{torch.cuda.get_device_name(dev)}:{name}:{probe}")
     g = tracer.graph(*ins, dt, steps, t0=t0, config=cfg)
     out = g.out
     counts = np.random.default_rng(4004).integers(nominal // 2, cap + 1,
@@ -650,14 +654,15 @@ def north_star_batched(args, dev, stream, flush) -> dict:
     traj, nr = fp64_trajectories(b, c, erays, t0, dt, steps, dev, stream)
     rel, dth = chunked_endpoint_errors(end_b, nst_b, traj, nr)
     # the FP64 model's own sensitivity: its endpoint change when the start
-    # moves 1 cm along x (sens), and the largest change under that, a 1e-6 rad
-    # turn and a 1e-6 relative change of |k| (worst: NaN where a perturbed ray
-    # ends at another step)
+    # moves 10 cm along x (sens), and the largest change under that, a 1e-5
+    # rad turn and a 1e-5 relative change of |k| -- perturbations of the size
+    # FP32 rounding accumulates to over a long trace (worst: NaN where a
+    # perturbed ray ends at another step)
     th, kk = torch.atan2(erays[3], erays[2]), torch.hypot(erays[2], erays[3])
     worst = None
-    for start in ([erays[0] + 0.01] + erays[1:],
-                  erays[:2] + [kk * torch.cos(th + 1e-6), kk * torch.sin(th + 1e-6)],
-                  erays[:2] + [erays[2] * (1.0 + 1e-6), erays[3] * (1.0 + 1e-6)]):
+    for start in ([erays[0] + 0.1] + erays[1:],
+                  erays[:2] + [kk * torch.cos(th + 1e-5), kk * torch.sin(th + 1e-5)],
+                  erays[:2] + [erays[2] * (1.0 + 1e-5), erays[3] * (1.0 + 1e-5)]):
         traj_p, nr_p = fp64_trajectories(b, c, start, t0, dt, steps, dev, stream)
         end_p, last_p = last_finite_states(traj_p, nr_p)
         del traj_p
@@ -699,7 +704,7 @@ def north_star_batched(args, dev, stream, flush) -> dict:
         "rays_per_call": {"min": int(timed_counts.min()), "max": int(timed_counts.max()),
                           "mean": float(timed_counts.mean()), "capacity": cap},
         "ray_steps_per_call": done / args.ns_calls, "max_steps": steps, "dt": dt,
-        "graph_replay": True, "launch": cfg.as_dict(), "autotuned": True,
+        "graph_replay": True, "launch": cfg.as_dict(), "autotuned": not args.launch,
         "field": f"{args.ns_grid}^2 f32 cell records (h, u, v, gradients), generated in "
                  f"{t_gen:.0f} s on the host",
         "l2": "512 MB buffer written between timed calls; cell records 5.4 GB > L2",
@@ -717,9 +722,9 @@ def north_star_batched(args, dev, stream, flush) -> dict:
             "fp64_conditioned_rays": dict(
                 error_stats(rel, dth, cond), share_of_rays=float(np.mean(cond)),
                 which="rays whose FP64 endpoint moves by <= 1e-4 of its path under each of "
-                      "three start perturbations: 1 cm along x, 1e-6 rad, 1e-6 of |k|"),
+                      "three start perturbations: 10 cm along x, 1e-5 rad, 1e-5 of |k|"),
             "target_rel_position": "<= 1e-3"},
-        "fp64_endpoint_change_for_1cm_start_shift": {
+        "fp64_endpoint_change_for_10cm_start_shift": {
             "rel_position_p50": float(np.nanmedian(sens)),
             "rel_position_p99": float(np.nanpercentile(sens, 99)),
             "rel_position_max": float(np.nanmax(sens))},
@@ -858,8 +863,8 @@ def batched_arm(args, rank: int, world: int, local_rank: int):
     cfg = default_config()
     tuned = None
     if args.launch:
-        blk, bps, rpl, order = (int(v) for v in args.launch.split(","))
-        cfg = make_config(blk, bps, rpl, 32, order)
+        blk, bps, rpl, order, *tile = (int(v) for v in args.launch.split(","))
+        cfg = make_config(blk, bps, rpl, 32, order, tile[0] if tile else 0)
     elif not args.no_autotune:
         probe = min(n_all, 1 << 20)
         pin = [t[:probe] for t in ins]

