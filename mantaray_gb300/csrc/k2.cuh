@@ -153,23 +153,32 @@ struct RayLane {
 //   tanh a = m / (2 - m),  a / cosh^2 a = 4 a q / (2 - m)^2,
 //   1 / (sinh a cosh a) = 4 q / (m (2 - m)),
 //   c_g = (g/2) (tanh a + a / cosh^2 a) / sqrt(g k tanh a),
-//   dk/dt from the depth = -(k/2) sqrt(g k tanh a) / (sinh a cosh a) grad h.
+//   dk/dt from the depth = -(k/2) sqrt(g k tanh a) / (sinh a cosh a) grad h;
+// beyond a = 23 (deep water) c_g = (g/2) / sqrt(g k) and no refraction.
 __device__ __forceinline__ void ray_equations(float h, float u, float v, float dudx, float dudy,
                                               float dvdx, float dvdy, float bx, float by,
                                               float kx, float ky, float k2, float d[4]) {
   const float rk = rsqrt_approx(k2);
   const float k = k2 * rk;
   const float kh = k * h;
-  float m, q;
-  one_minus_exp(-2.0f * kh, m, q);
-  const float inv_d = rcp_approx(m * (2.0f - m));  // 1 / (m (2 - m))
-  const float r = m * inv_d;            // 1 / (2 - m)
-  const float th = m * r;               // tanh(kh)
-  const float gkt = kGf * k * th;
-  const float rs = rsqrt_approx(gkt);
-  const float q4 = 4.0f * q;
-  const float cg = (0.5f * kGf) * (fmaf(kh * q4, r * r, th) * rs);
-  const float f = (-0.5f * k) * ((q4 * inv_d) * (gkt * rs));
+  float cg, f;
+  if (kh > 23.0f) {
+    // deep water: exp(-2kh) < 1e-20, so tanh(kh) = 1 and the terms in
+    // exp(-2kh) (kh / cosh^2, the refraction factor) vanish
+    cg = (0.5f * kGf) * rsqrt_approx(kGf * k);
+    f = 0.0f;
+  } else {
+    float m, q;
+    one_minus_exp(-2.0f * kh, m, q);
+    const float inv_d = rcp_approx(m * (2.0f - m));  // 1 / (m (2 - m))
+    const float r = m * inv_d;            // 1 / (2 - m)
+    const float th = m * r;               // tanh(kh)
+    const float gkt = kGf * k * th;
+    const float rs = rsqrt_approx(gkt);
+    const float q4 = 4.0f * q;
+    cg = (0.5f * kGf) * (fmaf(kh * q4, r * r, th) * rs);
+    f = (-0.5f * k) * ((q4 * inv_d) * (gkt * rs));
+  }
   const float cgk = cg * rk;            // c_g / k: c_g cos(theta) = cgk kx
   d[0] = fmaf(cgk, kx, u);
   d[1] = fmaf(cgk, ky, v);

@@ -19,9 +19,10 @@
 //    exp(-2kh) falls below the rounding of 1 - exp(-2kh) (kh > ~18): q then
 //    comes out 0 (or a multiple of 2^-53) instead of its true value below
 //    1e-16, so the refraction term f ~ q is off by up to that amount -- a
-//    change of k below one ulp of kx, ky per step.  Beyond kh = 22 the
-//    values m = 1, q = 0 are taken directly (what expm1 rounds to there),
-//    without the expm1 and the reciprocal.
+//    change of k below one ulp of kx, ky per step.  Beyond kh = 22 (where
+//    expm1 rounds to exactly -1) the deep-water forms are taken directly:
+//    c_g = (g/2) / sqrt(g k) and no refraction term, without the expm1, the
+//    reciprocal and the products by zero.
 // Both read the field values through the exact lookups, convert between f32
 // and f64 on the integer pipe (bits.h) and test NaN / zero on bit patterns,
 // which gives the same values as the conversion and comparison instructions.
@@ -103,19 +104,31 @@ struct RhsIdentity {
     // group_velocity's k <= 0 error (h > 0 or NaN): k is >= 0 or NaN here
     if (!(hg[0] <= 0.0f) && (__double_as_longlong(k) << 1) == 0) return RHS_ARGUMENT_OUT_OF_BOUNDS;
     const double a = k * h;
-    double m, q, w, r, th;
-    if (a > 22.0) {
+    // the deep-water form needs finite gradients (a NaN one makes the general
+    // form's refraction term NaN, which stops the ray as in the reference)
+    // and a finite depth
+    const uint32_t gx = bits_of(hg[1]), gy = bits_of(hg[2]);
+    if (a > 22.0 && a < 1.0e300 && (gx & 0x7f800000u) != 0x7f800000u &&
+        (gy & 0x7f800000u) != 0x7f800000u) {
       // deep water: exp(-2a) < 8e-20, far below half an ulp of 1, so
-      // -expm1(-2a) rounds to exactly 1 and every quantity below follows
-      // exactly: no expm1, no reciprocal
-      m = 1.0; q = 0.0; w = 1.0; r = 1.0; th = 1.0;
-    } else {
-      m = -expm1(-2.0 * a);                         // 1 - q
-      q = 1.0 - m;                                  // exp(-2a)
-      w = __drcp_rn(m * (2.0 - m));                 // 1 / (m (1 + q))
-      r = m * w;                                    // 1 / (1 + q)
-      th = m * r;                                   // tanh a
+      // -expm1(-2a) rounds to exactly 1: tanh a = 1, and the terms in
+      // exp(-2a) (a / cosh^2 a, the refraction factor f) are exactly 0 in the
+      // general branch too.  c_g and the current's terms are the general
+      // branch's bits; the refraction term is dropped rather than added as
+      // a signed zero.
+      const double rs = rsqrt(kG * k);              // 1 / sqrt(g k)
+      const double cg = (kG / 2.0) * rs;            // h > 0 here
+      out[0] = fma(cg, kx * rk, cur[0]);
+      out[1] = fma(cg, ky * rk, cur[1]);
+      out[2] = -fma(kx, cur[2], ky * cur[4]);
+      out[3] = -fma(kx, cur[3], ky * cur[5]);
+      return RHS_OK;
     }
+    const double m = -expm1(-2.0 * a);              // 1 - q
+    const double q = 1.0 - m;                       // exp(-2a)
+    const double w = __drcp_rn(m * (2.0 - m));      // 1 / (m (1 + q))
+    const double r = m * w;                         // 1 / (1 + q)
+    const double th = m * r;                        // tanh a
     const double gkt = (kG * k) * th;
     const double rs = rsqrt(gkt);                   // 1 / sqrt(g k tanh)
     const double q4 = 4.0 * q;
