@@ -102,7 +102,7 @@ def parse():
     p.add_argument("--no-autotune", action="store_true")
     p.add_argument("--launch", default=None,
                    help="batched form: fixed launch shape 'block,blocks_per_sm,rays_per_lane,"
-                        "order[,tile]' instead of the autotuner's")
+                        "order[,staging]' instead of the autotuner's")
     # the target measurements reported beside the plain form's line
     p.add_argument("--no-north-star", action="store_true",
                    help="plain form: skip the shelf-slope batched-vs-plain and adjoint-vs-"
@@ -615,11 +615,14 @@ def north_star_batched(args, dev, stream, flush) -> dict:
             f"{steps}steps_graph_replay")
     probe = min(cap, 1 << 20)
     if args.launch:
-        blk, bps, rpl, order, *tile = (int(v) for v in args.launch.split(","))
-        cfg = make_config(blk, bps, rpl, 32, order, tile[0] if tile else 0)
+        blk, bps, rpl, order, *stg = (int(v) for v in args.launch.split(","))
+        cfg = make_config(blk, bps, rpl, 32, order, stg[0] if stg else 0)
     else:
+        # short probe for every shape, then the fastest six again over a
+        # long trace, where the rays have spread over the whole field
         cfg = tracer.autotune(*[t[:probe] for t in ins], dt, min(steps, 1000), t0=t0,
-                              cache_key=f"{torch.cuda.get_device_name(dev)}:{name}:{probe}")
+                              cache_key=f"{torch.cuda.get_device_name(dev)}:{name}:{probe}",
+                              long_steps=min(steps, 10000), long_rays=probe, finalists=6)
     g = tracer.graph(*ins, dt, steps, t0=t0, config=cfg)
     out = g.out
     counts = np.random.default_rng(4004).integers(nominal // 2, cap + 1,
@@ -863,8 +866,8 @@ def batched_arm(args, rank: int, world: int, local_rank: int):
     cfg = default_config()
     tuned = None
     if args.launch:
-        blk, bps, rpl, order, *tile = (int(v) for v in args.launch.split(","))
-        cfg = make_config(blk, bps, rpl, 32, order, tile[0] if tile else 0)
+        blk, bps, rpl, order, *stg = (int(v) for v in args.launch.split(","))
+        cfg = make_config(blk, bps, rpl, 32, order, stg[0] if stg else 0)
     elif not args.no_autotune:
         probe = min(n_all, 1 << 20)
         pin = [t[:probe] for t in ins]

@@ -207,15 +207,24 @@ typedef struct mr_batch_config {
   int order;           /* 1: sort the rays by starting cell and direction before
                           tracing, so a warp's rays share cell records (results
                           per ray are unchanged); 0: trace in index order */
-  int tile;            /* 1: each warp keeps an 8 x 8-cell tile of the cell
-                          records in shared memory, loaded by the tensor memory
-                          accelerator and moved to where most of its rays are;
-                          a ray entering a cell of the tile reads it there
-                          (results per ray are unchanged).  One scenario with
-                          its current gridded on the bathymetry's grid only
-                          (MR_ERR_INVALID_ARGUMENT otherwise); 0: cell records
-                          from global memory */
+  int staging;         /* where a ray entering a new cell gets the cell's records
+                          (results per ray are the same for every choice):
+                          MR_STAGING_NONE from global memory;
+                          MR_STAGING_TILE from the warp's 8 x 8-cell tile in
+                          shared memory, loaded by the tensor memory
+                          accelerator and moved to where most of its rays are
+                          (one scenario with its current gridded on the
+                          bathymetry's grid only);
+                          MR_STAGING_AHEAD from registers loaded a step ahead
+                          with the cell the ray is heading into (every
+                          scenario's current gridded on its bathymetry's grid).
+                          Other combinations: MR_ERR_INVALID_ARGUMENT.  One ray
+                          per lane. */
 } mr_batch_config;
+
+#define MR_STAGING_NONE 0
+#define MR_STAGING_TILE 1
+#define MR_STAGING_AHEAD 2
 
 /* Per-ray status of the batched form. */
 #define MR_BATCH_COMPLETE 0       /* max_steps steps taken */

@@ -42,6 +42,10 @@ SYMBOLS = (
 
 SEED_EVEN_DIRECTIONS = 0x1
 
+STAGING_NONE = 0
+STAGING_TILE = 1
+STAGING_AHEAD = 2
+
 BATCH_STATIC_MAX_SCENARIOS = 64
 
 BATCH_COMPLETE = 0
@@ -62,7 +66,7 @@ class BatchConfig(ctypes.Structure):
 
     _fields_ = [("block", ctypes.c_int), ("blocks_per_sm", ctypes.c_int),
                 ("rays_per_lane", ctypes.c_int), ("rebase_interval", ctypes.c_int),
-                ("order", ctypes.c_int), ("tile", ctypes.c_int)]
+                ("order", ctypes.c_int), ("staging", ctypes.c_int)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}

@@ -33,8 +33,8 @@ def default_config() -> N.BatchConfig:
 
 
 def make_config(block=128, blocks_per_sm=4, rays_per_lane=1, rebase_interval=32,
-                order=0, tile=0) -> N.BatchConfig:
-    return N.BatchConfig(block, blocks_per_sm, rays_per_lane, rebase_interval, order, tile)
+                order=0, staging=0) -> N.BatchConfig:
+    return N.BatchConfig(block, blocks_per_sm, rays_per_lane, rebase_interval, order, staging)
 
 
 @dataclass
@@ -62,14 +62,15 @@ class BatchTracer:
         N.check(L.mr_batch_create(n, bs, cs, ctypes.byref(out)))
         self._h = out
         self.n_scenarios = n
-        self._tiles = None
+        self._staging = {}
 
-    @property
-    def tiles_supported(self) -> bool:
-        """Whether mr_batch_config.tile = 1 is accepted: one scenario with its
-        current gridded on the bathymetry's grid (tried once with a call of
-        no rays, which checks the configuration and traces nothing)."""
-        if self._tiles is None:
+    def supports(self, staging: int) -> bool:
+        """Whether mr_batch_config.staging = `staging` is accepted for this
+        batch (tried once per value with a call of no rays, which checks the
+        configuration and traces nothing): tiles need one scenario with its
+        current gridded on the bathymetry's grid, staging ahead every
+        scenario's current on its bathymetry's grid."""
+        if staging not in self._staging:
             torch = _torch()
             z = torch.empty(0, dtype=torch.float64, device="cuda")
             out = self.alloc(0, 1, 0, device="cuda")
@@ -77,9 +78,13 @@ class BatchTracer:
                 self._h, 0, None, z.data_ptr(), z.data_ptr(), z.data_ptr(), z.data_ptr(), 0.0,
                 1.0, 1, 0, 0, None, out.end_state.data_ptr(), out.n_steps.data_ptr(),
                 out.n_saved.data_ptr(), out.status.data_ptr(),
-                ctypes.byref(make_config(128, 4, 1, 32, 0, 1)), None)
-            self._tiles = rc == N.OK
-        return self._tiles
+                ctypes.byref(make_config(128, 4, 1, 32, 0, staging)), None)
+            self._staging[staging] = rc == N.OK
+        return self._staging[staging]
+
+    @property
+    def tiles_supported(self) -> bool:
+        return self.supports(N.STAGING_TILE)
 
     def close(self):
         if self._h and self._h.value:
@@ -130,11 +135,16 @@ class BatchTracer:
                           config or default_config())
 
     def autotune(self, x0, y0, kx0, ky0, dt, probe_steps, t0=0.0, scenario=None,
-                 candidates=None, repeats=2, cache_key=None) -> N.BatchConfig:
+                 candidates=None, repeats=2, cache_key=None, long_steps=None,
+                 long_rays=None, finalists=4) -> N.BatchConfig:
         """Times every candidate launch shape on a probe run (the given rays
         for `probe_steps` steps, endpoints only) and returns the fastest.
-        Results are cached in memory and in $MANTARAY_TUNE_CACHE (a JSON file)
-        when that is set."""
+        With `long_steps`, the `finalists` fastest are timed again on the
+        first `long_rays` rays for `long_steps` steps, once each, and the
+        fastest of that run wins: a short probe keeps the rays near their
+        starts, where the fields they read may fit in L2, while a long trace
+        spreads them over the whole field.  Results are cached in memory and
+        in $MANTARAY_TUNE_CACHE (a JSON file) when that is set."""
         torch = _torch()
         key = cache_key
         cache_path = os.environ.get("MANTARAY_TUNE_CACHE")
@@ -151,28 +161,43 @@ class BatchTracer:
                                                                       (2, 4, 6, 8, 12),
                                                                       (1, 2), (0, 1))
                           if b * bps <= 2048]
-            if self.tiles_supported:
-                # shared-memory tiles of cell records (one ray per lane, ordered rays)
-                candidates += [make_config(b, bps, 1, 32, 1, 1)
-                               for b, bps in itertools.product((64, 128, 256), (2, 4, 6, 8, 12))
-                               if b * bps <= 2048]
-        out = self.alloc(int(x0.numel()), probe_steps, 0, device=x0.device)
-        best, best_t = None, float("inf")
+            # staged cell records (one ray per lane): shared-memory tiles
+            # (ordered rays), records loaded ahead
+            for staging, orders in ((N.STAGING_TILE, (1,)), (N.STAGING_AHEAD, (0, 1))):
+                if self.supports(staging):
+                    candidates += [make_config(b, bps, 1, 32, order, staging)
+                                   for b, bps, order in itertools.product(
+                                       (64, 128, 256), (2, 4, 6, 8, 12), orders)
+                                   if b * bps <= 2048]
         stream = torch.cuda.current_stream(x0.device)
-        for cfg in candidates:
-            self.trace(x0, y0, kx0, ky0, dt, probe_steps, t0, 0, scenario, cfg, out, stream)
-            times = []
-            for _ in range(repeats):
+
+        def timed(cfg, rays, steps, reps, out):
+            self.trace(*rays, dt, steps, t0, 0, sc(rays), cfg, out, stream)
+            ts = []
+            for _ in range(reps):
                 e0 = torch.cuda.Event(enable_timing=True)
                 e1 = torch.cuda.Event(enable_timing=True)
                 e0.record(stream)
-                self.trace(x0, y0, kx0, ky0, dt, probe_steps, t0, 0, scenario, cfg, out, stream)
+                self.trace(*rays, dt, steps, t0, 0, sc(rays), cfg, out, stream)
                 e1.record(stream)
                 e1.synchronize()
-                times.append(e0.elapsed_time(e1))
-            t = min(times)
-            if t < best_t:
-                best, best_t = cfg, t
+                ts.append(e0.elapsed_time(e1))
+            return min(ts)
+
+        def sc(rays):
+            return None if scenario is None else scenario[: rays[0].numel()]
+
+        rays = (x0, y0, kx0, ky0)
+        out = self.alloc(int(x0.numel()), probe_steps, 0, device=x0.device)
+        ranked = sorted((timed(cfg, rays, probe_steps, repeats, out), i)
+                        for i, cfg in enumerate(candidates))
+        best = candidates[ranked[0][1]]
+        if long_steps:
+            m = int(min(x0.numel(), long_rays or x0.numel()))
+            rays = tuple(t[:m] for t in rays)
+            out = self.alloc(m, long_steps, 0, device=x0.device)
+            finals = [candidates[i] for _, i in ranked[:finalists]]
+            best = min(finals, key=lambda cfg: timed(cfg, rays, long_steps, 1, out))
         if key:
             _TUNE_CACHE[key] = best.as_dict()
             if cache_path:

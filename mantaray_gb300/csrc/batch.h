@@ -61,7 +61,7 @@ struct BatchArgs {
   // [ny-1][nx-1][8 floats], current [ny-1][nx-1][12 floats]
   CUtensorMap tmap_bathy;
   CUtensorMap tmap_current;
-  int tile;                  // 1: the tile build
+  int staging;               // MR_STAGING_* (the tile and ahead builds)
   const ScenarioDev *scen;   // [n_scenarios]
   ScenarioDev scen0;         // scen[0] by value: the single-scenario build reads it from
                              // the kernel's parameters, with no load

@@ -196,10 +196,10 @@ int check_config(const mr_batch_config *cfg) {
     return fail(MR_ERR_INVALID_ARGUMENT, "rebase_interval must be >= 1");
   if (cfg->order != 0 && cfg->order != 1)
     return fail(MR_ERR_INVALID_ARGUMENT, "order must be 0 or 1");
-  if (cfg->tile != 0 && cfg->tile != 1)
-    return fail(MR_ERR_INVALID_ARGUMENT, "tile must be 0 or 1");
-  if (cfg->tile && cfg->rays_per_lane != 1)
-    return fail(MR_ERR_INVALID_ARGUMENT, "tile staging traces one ray per lane");
+  if (cfg->staging < MR_STAGING_NONE || cfg->staging > MR_STAGING_AHEAD)
+    return fail(MR_ERR_INVALID_ARGUMENT, "staging must be 0, 1 or 2");
+  if (cfg->staging && cfg->rays_per_lane != 1)
+    return fail(MR_ERR_INVALID_ARGUMENT, "staging traces one ray per lane");
   return MR_OK;
 }
 
@@ -242,11 +242,14 @@ int fill_args(mr_batch *b, size_t n, size_t n_stride, const uint8_t *ray_scenari
                   static_cast<long long>(max_steps / decimation + 1));
   }
   if (!(dt > 0.0) || !isfinite(t0)) return fail(MR_ERR_INVALID_ARGUMENT, "dt must be > 0");
-  if (cfg->tile && !b->has_tmaps)
+  if (cfg->staging == MR_STAGING_TILE && !b->has_tmaps)
     return fail(MR_ERR_INVALID_ARGUMENT,
                 "tile staging needs one scenario with its current gridded on the bathymetry's "
                 "grid");
-  a->tile = cfg->tile;
+  if (cfg->staging == MR_STAGING_AHEAD && !all_same_grid(b))
+    return fail(MR_ERR_INVALID_ARGUMENT,
+                "staging ahead needs every scenario's current gridded on its bathymetry's grid");
+  a->staging = cfg->staging;
   if (b->has_tmaps) {
     a->tmap_bathy = b->tmap_bathy;
     a->tmap_current = b->tmap_current;
@@ -328,7 +331,7 @@ int mr_batch_default_config(mr_batch_config *cfg) {
   cfg->rays_per_lane = 1;
   cfg->rebase_interval = 32;
   cfg->order = 0;
-  cfg->tile = 0;
+  cfg->staging = MR_STAGING_NONE;
   return MR_OK;
 }
 
@@ -465,7 +468,7 @@ int mr_batch_graph_create(mr_batch *b, size_t n_max, const uint8_t *ray_scenario
   // the integrator build for this shape, chosen (an occupancy query) before
   // the capture begins
   (void)mr::rk4_f32_function(cfg->rays_per_lane, cfg->block, cfg->blocks_per_sm,
-                             b->n_scenarios, all_same_grid(b), cfg->tile);
+                             b->n_scenarios, all_same_grid(b), cfg->staging);
   if (e == cudaSuccess) e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
     cudaError_t le = enqueue(b, a, cfg, &gr->ord, s);
@@ -489,7 +492,7 @@ int mr_batch_graph_create(mr_batch *b, size_t n_max, const uint8_t *ray_scenario
         gr->order_params = p;
       } else if (p.func == mr::rk4_f32_function(cfg->rays_per_lane, cfg->block,
                                                 cfg->blocks_per_sm, b->n_scenarios,
-                                                all_same_grid(b), cfg->tile)) {
+                                                all_same_grid(b), cfg->staging)) {
         gr->kernel_node = nodes[i];
         gr->params = p;
       }

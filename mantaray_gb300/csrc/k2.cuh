@@ -133,6 +133,15 @@ struct CellCache {
   float4 c0, c1, c2;      // u's and v's coefficients, the current's gradients
 };
 
+// The records of the cell a lane's ray is heading into (the ahead build),
+// loaded a step before the ray enters it.
+struct NextCell {
+  int key;                // cell index held, -1: none
+  float4 b0;
+  float bx, by;
+  float4 c0, c1, c2;
+};
+
 struct RayLane {
   int64_t ray;      // -1: empty slot, -2: no work left
   int scen;
@@ -145,6 +154,7 @@ struct RayLane {
   int32_t to_save;    // steps until the next decimated row (no 64-bit modulo per step)
   int32_t to_rebase;  // steps until the next origin rebase
   CellCache cache;
+  NextCell next;      // the ahead build only
 };
 
 // The ray equations in FP32 from the looked-up fields (bx, by: dh/dx,
@@ -220,6 +230,62 @@ __device__ __forceinline__ void load_same_grid_cell(const ScenarioDev &s, CellCa
     C.c2 = __ldg(s.current.cells + static_cast<int64_t>(cb) * 3 + 2);
     C.bkey = cb;
   }
+}
+
+// The records of cell cb of both fields (modes 2 and 3, the ahead build),
+// unless the lane holds them: from the registers loaded ahead when the ray
+// entered the cell it was predicted to enter.
+__device__ __forceinline__ void load_same_grid_cell_ahead(const ScenarioDev &s, CellCache &C,
+                                                          const NextCell &N, int cb) {
+  if (cb != C.bkey) {
+    if (cb == N.key) {
+      C.b0 = N.b0;
+      C.bx = N.bx;
+      C.by = N.by;
+      C.c0 = N.c0;
+      C.c1 = N.c1;
+      C.c2 = N.c2;
+      C.bkey = cb;
+    } else {
+      load_same_grid_cell(s, C, cb);
+    }
+  }
+}
+
+// The ahead build's prediction, once a step after the first stage: the
+// neighbour cell the ray leaves its cell into at velocity (vx, vy) (the
+// nearer of its x and y exits), whose records are loaded into L.next now;
+// they are first read when the ray enters that cell, a step or more later,
+// so the load's latency passes while the lane computes.
+template <int MODE>
+__device__ __forceinline__ void load_ahead(const ScenarioDev &s, RayLane &L, float vx, float vy) {
+  int cb, ix, iy;
+  float fx, fy;
+  if (!locate(s.bathy, L.pb, L.px, L.py, &cb, &fx, &fy, &ix, &iy)) return;
+  const float ux = vx * s.bathy.inv_sp_x, uy = vy * s.bathy.inv_sp_y;  // cells per second
+  const float tx = ux > 0.0f ? (1.0f - fx) * rcp_approx(ux)
+                             : (ux < 0.0f ? fx * rcp_approx(-ux) : 3.0e38f);
+  const float ty = uy > 0.0f ? (1.0f - fy) * rcp_approx(uy)
+                             : (uy < 0.0f ? fy * rcp_approx(-uy) : 3.0e38f);
+  int ni = ix, nj = iy;
+  if (tx < ty)
+    ni += ux > 0.0f ? 1 : -1;
+  else
+    nj += uy > 0.0f ? 1 : -1;
+  if (static_cast<unsigned>(ni) > static_cast<unsigned>(s.bathy.nx - 2) ||
+      static_cast<unsigned>(nj) > static_cast<unsigned>(s.bathy.ny - 2))
+    return;
+  const int key = nj * (s.bathy.nx - 1) + ni;
+  NextCell &N = L.next;
+  if (key == N.key || key == L.cache.bkey) return;
+  N.b0 = __ldg(s.bathy.cells + static_cast<int64_t>(key) * 2);
+  const float4 b1 = __ldg(s.bathy.cells + static_cast<int64_t>(key) * 2 + 1);
+  N.bx = b1.x;
+  N.by = b1.y;
+  N.c0 = __ldg(s.current.cells + static_cast<int64_t>(key) * 3);
+  N.c1 = __ldg(s.current.cells + static_cast<int64_t>(key) * 3 + 1);
+  N.c2 = __ldg(s.current.cells + static_cast<int64_t>(key) * 3 + 2);
+  N.key = key;
 }
 
 // ---------------------------------------------------- shared-memory tiles --
@@ -371,9 +437,10 @@ __device__ __forceinline__ void load_same_grid_cell_tile(const ScenarioDev &s, C
 // meaningful only when complete.  Written without early returns so that the
 // four stages of a step run with no branch between them.  MODE 2 and 3: the
 // current is gridded on the bathymetry's grid, so one cell (one key, one
-// test) serves both fields.  TILE (mode 2): records from the warp's tile
-// when the cell is in it.
-template <int MODE, bool EXACT, bool TILE>
+// test) serves both fields.  STAGE (MR_STAGING_*): 1 (mode 2), records from
+// the warp's tile when the cell is in it; 2 (modes 2, 3), from the registers
+// loaded ahead when the ray entered the predicted cell.
+template <int MODE, bool EXACT, int STAGE>
 __device__ __forceinline__ int rhs_f32(const ScenarioDev &s, RayLane &L, const WarpTile &W,
                                        float px, float py, float kx, float ky, float d[4]) {
   CellCache &C = L.cache;
@@ -382,8 +449,10 @@ __device__ __forceinline__ int rhs_f32(const ScenarioDev &s, RayLane &L, const W
   bool inside = locate(s.bathy, L.pb, px, py, &cb, &fx, &fy, &ix, &iy);
   float u, v, dudx, dudy, dvdx, dvdy;
   if (MODE == 2 || MODE == 3) {
-    if (TILE)
+    if (STAGE == 1)
       load_same_grid_cell_tile(s, C, W, inside ? cb : C.bkey, ix, iy);
+    else if (STAGE == 2)
+      load_same_grid_cell_ahead(s, C, L.next, inside ? cb : C.bkey);
     else
       load_same_grid_cell(s, C, inside ? cb : C.bkey);
     u = bilin(C.c0, fx, fy);
@@ -503,13 +572,13 @@ __device__ __forceinline__ void start(const BatchArgs &a, RayLane &L, int64_t r)
 // again, in order, up to the first that fails (the same arithmetic on the
 // same inputs, so the same values and the same first failure).  Taken once
 // per ray at most: the ray ends there.  One stage in a loop: little code.
-template <int MODE, bool TILE>
+template <int MODE, int STAGE>
 __device__ __forceinline__ int step_status(const ScenarioDev &s, RayLane &L, const WarpTile &W,
                                            float dt, float half) {
   float k[4], x[4] = {L.px, L.py, L.kx, L.ky};
 #pragma unroll 1
   for (int st = 0; st < 4; ++st) {
-    const int r = rhs_f32<MODE, true, TILE>(s, L, W, x[0], x[1], x[2], x[3], k);
+    const int r = rhs_f32<MODE, true, STAGE>(s, L, W, x[0], x[1], x[2], x[3], k);
     if (r != BATCH_COMPLETE) return r;
     const float w = st == 2 ? dt : half;
     x[0] = fmaf(w, k[0], L.px);
@@ -530,7 +599,7 @@ __device__ __forceinline__ int step_status(const ScenarioDev &s, RayLane &L, con
 // summed as the stages complete, so only the sum and the latest stage's
 // derivative stay live (register pressure, not arithmetic, bounds how many
 // warps an SM holds).
-template <int MODE, bool TILE>
+template <int MODE, int STAGE>
 __device__ __forceinline__ int advance(const BatchArgs &a, RayLane &L, const WarpTile &W) {
   const ScenarioDev &s = scenario<MODE>(a, L.scen);
   // step constants in FP32 from the host (a conversion here would run on the
@@ -538,20 +607,21 @@ __device__ __forceinline__ int advance(const BatchArgs &a, RayLane &L, const War
   const float dt = a.dt_f;
   const float half = a.half_f;
   float k[4], sum[4];
-  int fails = rhs_f32<MODE, false, TILE>(s, L, W, L.px, L.py, L.kx, L.ky, k);
+  int fails = rhs_f32<MODE, false, STAGE>(s, L, W, L.px, L.py, L.kx, L.ky, k);
 #pragma unroll
   for (int q = 0; q < 4; ++q) sum[q] = k[q];
-  fails |= rhs_f32<MODE, false, TILE>(s, L, W, fmaf(half, k[0], L.px), fmaf(half, k[1], L.py),
+  if (STAGE == 2) load_ahead<MODE>(s, L, k[0], k[1]);
+  fails |= rhs_f32<MODE, false, STAGE>(s, L, W, fmaf(half, k[0], L.px), fmaf(half, k[1], L.py),
                                 fmaf(half, k[2], L.kx), fmaf(half, k[3], L.ky), k);
 #pragma unroll
   for (int q = 0; q < 4; ++q) sum[q] = fmaf(2.0f, k[q], sum[q]);
-  fails |= rhs_f32<MODE, false, TILE>(s, L, W, fmaf(half, k[0], L.px), fmaf(half, k[1], L.py),
+  fails |= rhs_f32<MODE, false, STAGE>(s, L, W, fmaf(half, k[0], L.px), fmaf(half, k[1], L.py),
                                 fmaf(half, k[2], L.kx), fmaf(half, k[3], L.ky), k);
 #pragma unroll
   for (int q = 0; q < 4; ++q) sum[q] = fmaf(2.0f, k[q], sum[q]);
-  fails |= rhs_f32<MODE, false, TILE>(s, L, W, fmaf(dt, k[0], L.px), fmaf(dt, k[1], L.py),
+  fails |= rhs_f32<MODE, false, STAGE>(s, L, W, fmaf(dt, k[0], L.px), fmaf(dt, k[1], L.py),
                                 fmaf(dt, k[2], L.kx), fmaf(dt, k[3], L.ky), k);
-  if (fails != BATCH_COMPLETE) return step_status<MODE, TILE>(s, L, W, dt, half);
+  if (fails != BATCH_COMPLETE) return step_status<MODE, STAGE>(s, L, W, dt, half);
   const float sixth = a.sixth_f;
   kahan_add(L.px, L.cpx, sixth * (sum[0] + k[0]));
   kahan_add(L.py, L.cpy, sixth * (sum[1] + k[1]));
@@ -590,7 +660,7 @@ __device__ __forceinline__ void tile_refresh(const BatchArgs &a, const RayLane &
   tile_load(a, W, ti, tj);
 }
 
-template <int RPT, int MODE, bool TILE>
+template <int RPT, int MODE, int STAGE>
 __device__ __forceinline__ void k2_body(const BatchArgs &a) {
   const int lane = threadIdx.x & 31;
   const unsigned lt_mask = (1u << lane) - 1u;
@@ -600,7 +670,7 @@ __device__ __forceinline__ void k2_body(const BatchArgs &a) {
 #pragma unroll
   for (int j = 0; j < RPT; ++j) L[j].ray = -1;
   WarpTile W;
-  if (TILE) W = tile_init();
+  if (STAGE == 1) W = tile_init();
   int iter = 0;
   while (true) {
     // refill empty slots from the work queue, one atomic per warp and slot
@@ -614,8 +684,12 @@ __device__ __forceinline__ void k2_body(const BatchArgs &a) {
         base = __shfl_sync(kFull, base, leader);
         if (L[j].ray == -1) {
           const int64_t r = static_cast<int64_t>(base) + __popc(need & lt_mask);
-          if (r < n) start<MODE>(a, L[j], a.order ? static_cast<int64_t>(__ldg(a.order + r)) : r);
-          else L[j].ray = -2;
+          if (r < n) {
+            start<MODE>(a, L[j], a.order ? static_cast<int64_t>(__ldg(a.order + r)) : r);
+            if (STAGE == 2) L[j].next.key = -1;
+          } else {
+            L[j].ray = -2;
+          }
         }
       }
     }
@@ -623,7 +697,7 @@ __device__ __forceinline__ void k2_body(const BatchArgs &a) {
 #pragma unroll
     for (int j = 0; j < RPT; ++j) live |= L[j].ray >= 0;
     if (!__any_sync(kFull, live)) break;
-    if (TILE && (iter++ & 3) == 0) tile_refresh<MODE>(a, L[0], W);
+    if (STAGE == 1 && (iter++ & 3) == 0) tile_refresh<MODE>(a, L[0], W);
 #pragma unroll
     for (int j = 0; j < RPT; ++j) {
       if (L[j].ray < 0) continue;
@@ -631,11 +705,11 @@ __device__ __forceinline__ void k2_body(const BatchArgs &a) {
         finish(a, L[j], BATCH_COMPLETE);
         continue;
       }
-      const int st = advance<MODE, TILE>(a, L[j], W);
+      const int st = advance<MODE, STAGE>(a, L[j], W);
       if (st != BATCH_COMPLETE) finish(a, L[j], st);
     }
   }
-  if (TILE) tile_finish(W);
+  if (STAGE == 1) tile_finish(W);
 }
 
 // One ray per lane, two builds.  rk4_f32_kernel_1 takes the compiler's
@@ -655,12 +729,12 @@ __device__ __forceinline__ void k2_body(const BatchArgs &a) {
 // lookup); 2 is mode 1 and 3 is mode 0 with the current gridded on the
 // bathymetry's grid (every scenario's, for 3).
 template <int MODE>
-__global__ void __launch_bounds__(256) rk4_f32_kernel_1(BatchArgs a) { k2_body<1, MODE, false>(a); }
+__global__ void __launch_bounds__(256) rk4_f32_kernel_1(BatchArgs a) { k2_body<1, MODE, 0>(a); }
 template <int MODE>
-__global__ void __maxnreg__(72) rk4_f32_kernel_1r(BatchArgs a) { k2_body<1, MODE, false>(a); }
+__global__ void __maxnreg__(72) rk4_f32_kernel_1r(BatchArgs a) { k2_body<1, MODE, 0>(a); }
 // Two rays per lane hold twice the lane state: no cap.
 template <int MODE>
-__global__ void __launch_bounds__(256) rk4_f32_kernel_2(BatchArgs a) { k2_body<2, MODE, false>(a); }
+__global__ void __launch_bounds__(256) rk4_f32_kernel_2(BatchArgs a) { k2_body<2, MODE, 0>(a); }
 // The tile build (mode 2): one ray per lane (the compiler's register count,
 // 80; capped at 72 it spilled), each warp's tile in dynamic
 // shared memory (kTileBytes per warp, then 8 bytes of mbarrier per warp); the
@@ -668,8 +742,12 @@ __global__ void __launch_bounds__(256) rk4_f32_kernel_2(BatchArgs a) { k2_body<2
 // copies read the tensor maps from there.
 template <int MODE>
 __global__ void __launch_bounds__(256) rk4_f32_kernel_1t(const __grid_constant__ BatchArgs a) {
-  k2_body<1, MODE, true>(a);
+  k2_body<1, MODE, 1>(a);
 }
+// The ahead build (modes 2 and 3): one ray per lane, with the records of the
+// cell each ray heads into loaded a step early (20 more registers a lane).
+template <int MODE>
+__global__ void __launch_bounds__(256) rk4_f32_kernel_1a(BatchArgs a) { k2_body<1, MODE, 2>(a); }
 
 }  // namespace
 

@@ -35,15 +35,15 @@ cudaError_t launch_rk4_f32(const BatchArgs &a, int block, int blocks_per_sm, int
                            cudaStream_t stream);
 // The integrator build a launch of this shape runs, for n_scenarios
 // scenarios (same_grid: every scenario's current is gridded on its
-// bathymetry's grid; tile: the shared-memory tile build, one scenario on the
-// same grid only, else null); a graph's kernel node is found by it.
+// bathymetry's grid; staging: MR_STAGING_*, null where that build does not
+// exist); a graph's kernel node is found by it.
 const void *rk4_f32_function(int rays_per_lane, int block, int blocks_per_sm, int n_scenarios,
-                             int same_grid, int tile);
+                             int same_grid, int staging);
 // Dynamic shared memory of the tile build for blocks of `block` threads.
 size_t rk4_f32_tile_smem(int block);
 // The single-scenario builds (rk4_f32_one.cu): 0 one ray per lane, 1 the same
-// capped at 72 registers, 2 two rays per lane, 3 the tile build (same grid
-// only, else null).
+// capped at 72 registers, 2 two rays per lane, 3 the tile build, 4 the ahead
+// build (3 and 4: same grid only, else null).
 const void *rk4_f32_one_function(int build, int same_grid);
 cudaError_t launch_fill_nan(float *p, int64_t count, cudaStream_t stream);
 

@@ -167,9 +167,15 @@ size_t rk4_f32_tile_smem(int block) {
 }
 
 const void *rk4_f32_function(int rays_per_lane, int block, int blocks_per_sm, int n_scenarios,
-                             int same_grid, int tile) {
+                             int same_grid, int staging) {
   const int mode = n_scenarios == 1 ? (same_grid ? 2 : 1) : (same_grid ? 3 : 0);
-  if (tile) return (mode == 2 && rays_per_lane == 1) ? rk4_f32_one_function(3, 1) : nullptr;
+  if (staging == 1) return (mode == 2 && rays_per_lane == 1) ? rk4_f32_one_function(3, 1) : nullptr;
+  if (staging == 2) {
+    if (rays_per_lane != 1) return nullptr;
+    if (mode == 2) return rk4_f32_one_function(4, 1);
+    if (mode == 3) return reinterpret_cast<const void *>(&rk4_f32_kernel_1a<3>);
+    return nullptr;
+  }
   const void *fn[3];
   for (int k = 0; k < 3; ++k)
     fn[k] = (mode == 1 || mode == 2) ? rk4_f32_one_function(k, mode == 2)
@@ -200,10 +206,10 @@ cudaError_t launch_rk4_f32(const BatchArgs &a, int block, int blocks_per_sm, int
   const unsigned grid = static_cast<unsigned>(sms * blocks_per_sm);
   void *args[] = {const_cast<BatchArgs *>(&a)};
   const void *fn = rk4_f32_function(rays_per_lane, block, blocks_per_sm, a.n_scenarios,
-                                    a.all_same_grid, a.tile);
+                                    a.all_same_grid, a.staging);
   if (!fn) return cudaErrorInvalidValue;
-  return cudaLaunchKernel(fn, dim3(grid), dim3(block), args, a.tile ? rk4_f32_tile_smem(block) : 0,
-                          stream);
+  return cudaLaunchKernel(fn, dim3(grid), dim3(block), args,
+                          a.staging == 1 ? rk4_f32_tile_smem(block) : 0, stream);
 }
 
 }  // namespace mr

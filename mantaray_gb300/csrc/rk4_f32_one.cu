@@ -26,6 +26,7 @@ static const void *one_build(int build) {
 
 const void *rk4_f32_one_function(int build, int same_grid) {
   if (build == 3) return same_grid ? reinterpret_cast<const void *>(&rk4_f32_kernel_1t<2>) : nullptr;
+  if (build == 4) return same_grid ? reinterpret_cast<const void *>(&rk4_f32_kernel_1a<2>) : nullptr;
   return same_grid ? one_build<2>(build) : one_build<1>(build);
 }
 

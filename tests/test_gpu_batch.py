@@ -522,12 +522,15 @@ def test_decimation_tuner_budgets(mr):
         tracer.tune_decimation(*ins, w.dt, 400, (1, 10), 1 << 20)
 
 
+@pytest.mark.parametrize("staging", [1, 2])
 @pytest.mark.parametrize("field", ["seamount", "shelf_slope"])
-def test_tiles_give_identical_results(mr, field):
-    # Shared-memory tiles of the cell records (copied in by the tensor memory
-    # accelerator) change where a lane reads a cell's records, not their
-    # values: every output bit equals the untiled build's, for several launch
-    # shapes and through a captured graph.
+def test_staging_gives_identical_results(mr, field, staging):
+    # Staged cell records -- shared-memory tiles copied in by the tensor
+    # memory accelerator (1), or the records of the cell each ray heads into
+    # loaded into registers a step ahead (2) -- change where a lane reads a
+    # cell's records, not their values: every output bit equals the
+    # unstaged build's, for several launch shapes and through a captured
+    # graph.
     from mantaray_gb300.batch import BatchTracer, make_config
     from mantaray_gb300.workloads import seamount, shelf_slope
 
@@ -541,7 +544,7 @@ def test_tiles_give_identical_results(mr, field):
         c = mr.Current.grid(f[3], f[4], f[5], f[6])
         rays, dt, steps = (r["x0"], r["y0"], r["kx0"], r["ky0"]), r["dt"], 2000
     tracer = BatchTracer([(b, c)])
-    assert tracer.tiles_supported
+    assert tracer.supports(staging)
     ins = _dev(*rays)
 
     def bits(o):
@@ -549,18 +552,42 @@ def test_tiles_give_identical_results(mr, field):
                 o.status.cpu().numpy(), o.saved.cpu().numpy().view(np.uint32)]
 
     ref = bits(tracer.trace(*ins, dt, steps, decimation=50, config=make_config(128, 4, 1, 32, 1)))
-    for shape in ((128, 4, 1, 32, 1, 1), (64, 8, 1, 32, 1, 1), (256, 2, 1, 32, 0, 1)):
-        got = bits(tracer.trace(*ins, dt, steps, decimation=50, config=make_config(*shape)))
+    for shape in ((128, 4, 1, 32, 1), (64, 8, 1, 32, 1), (256, 2, 1, 32, 0)):
+        got = bits(tracer.trace(*ins, dt, steps, decimation=50,
+                                config=make_config(*shape, staging)))
         for x, y in zip(got, ref):
             np.testing.assert_array_equal(x, y)
-    g = tracer.graph(*ins, dt, steps, decimation=50, config=make_config(128, 6, 1, 32, 1, 1))
+    g = tracer.graph(*ins, dt, steps, decimation=50, config=make_config(128, 6, 1, 32, 1, staging))
     g.launch()
     for x, y in zip(bits(g.out), ref):
         np.testing.assert_array_equal(x, y)
     g.close()
 
 
-def test_tiles_refused_where_they_do_not_apply(mr):
+def test_staging_ahead_across_scenarios(mr):
+    # the ahead build of the scenario-table form (mode 3, every current on its
+    # bathymetry's grid): the same bits as the unstaged build
+    from mantaray_gb300.batch import BatchTracer, make_config
+    from mantaray_gb300.workloads import multi_source
+
+    scen, rays = multi_source(n_sources=32, rays_per_source=128, n_scenarios=4, n=512,
+                              steps=1500)
+    tracer = BatchTracer([(mr.Bathymetry.grid(*s[:3]), mr.Current.grid(*s[3:])) for s in scen])
+    assert tracer.supports(2) and not tracer.supports(1)
+    ins = _dev(rays["x0"], rays["y0"], rays["kx0"], rays["ky0"])
+    (sid,) = _dev(rays["scenario"])
+    outs = [tracer.trace(*ins, rays["dt"], 1500, decimation=100, scenario=sid,
+                         config=make_config(128, 4, 1, 32, 0, st)) for st in (0, 2)]
+    for a, b_ in zip((outs[0].end_state, outs[0].n_steps, outs[0].status, outs[0].saved),
+                     (outs[1].end_state, outs[1].n_steps, outs[1].status, outs[1].saved)):
+        x, y = a.cpu().numpy(), b_.cpu().numpy()
+        if x.dtype in (np.float32, np.float64):
+            x, y = x.view(np.uint32 if x.dtype == np.float32 else np.uint64), \
+                y.view(np.uint32 if y.dtype == np.float32 else np.uint64)
+        np.testing.assert_array_equal(x, y)
+
+
+def test_staging_refused_where_it_does_not_apply(mr):
     from mantaray_gb300 import MantarayError
     from mantaray_gb300.batch import BatchTracer, make_config
 
@@ -575,5 +602,10 @@ def test_tiles_refused_where_they_do_not_apply(mr):
         assert not tr.tiles_supported
         with pytest.raises(MantarayError, match="tile staging"):
             tr.trace(*ins, 1.0, 10, config=make_config(128, 4, 1, 32, 0, 1))
+    assert two.supports(2) and not own.supports(2)
+    with pytest.raises(MantarayError, match="staging ahead"):
+        own.trace(*ins, 1.0, 10, config=make_config(128, 4, 1, 32, 0, 2))
+    with pytest.raises(MantarayError, match="staging must be"):
+        two.trace(*ins, 1.0, 10, config=make_config(128, 4, 1, 32, 0, 3))
     with pytest.raises(MantarayError, match="one ray per lane"):
         BatchTracer([(b, c)]).trace(*ins, 1.0, 10, config=make_config(128, 4, 2, 32, 0, 1))
