@@ -68,9 +68,15 @@ K1_DRAM_BYTES_PER_RAY_STEP = (55537408 + 2573673472) / (65536 * 1000)
 K1_DRAM_NOTE = ("ncu DRAM bytes of a 65,536-ray x 1,000-step launch of the same workload "
                 "(55.5 MB read, 2,573.7 MB written) scaled by ray-steps; rows still in L2 at the "
                 "end of that launch (at most 129 MB) are not counted")
-# The same for the batched kernel on the shelf-slope field.
-K2_SHELF_DRAM_BYTES_PER_RAY_STEP = None
-K2_SHELF_DRAM_NOTE = ""
+# The same for the batched kernel on the shelf-slope field: one graph-replayed
+# call of 262,144 rays traced to their ends on the field's generator at
+# 4,096^2 (records 1.3 GB, 10x L2; 3.10 G ray-steps; 161.04 GB read, 0.09 GB
+# written).  Its rays spread over the field as the benchmark's do on 8,192^2,
+# and a ray entering a new cell reads that cell's records from DRAM in both,
+# so the bytes scale with ray-steps.
+K2_SHELF_DRAM_BYTES_PER_RAY_STEP = (161042433536 + 93049344) / 3103336576
+K2_SHELF_DRAM_NOTE = ("ncu DRAM bytes of one call of the same generator at 4,096^2 (262,144 rays "
+                      "to their ends, 51.9 B per ray-step), scaled by this call's ray-steps")
 
 
 def parse():
@@ -698,6 +704,17 @@ def north_star_batched(args, dev, stream, flush) -> dict:
     if K2_SHELF_DRAM_BYTES_PER_RAY_STEP is not None:
         roof["traffic"] = K2_SHELF_DRAM_BYTES_PER_RAY_STEP * done / args.ns_calls
         roof["traffic_note"] = K2_SHELF_DRAM_NOTE
+        try:
+            hbm_peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
+            src = "MEASURED_PEAKS.json hbm_gbs"
+        except (OSError, ValueError, KeyError):
+            hbm_peak, src = 6800.0, "fallback"
+        gbs = K2_SHELF_DRAM_BYTES_PER_RAY_STEP * value / 1e9
+        roof["hbm"] = {"achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
+                       "peak_source": src,
+                       "note": "the DRAM reads of cell records on cell changes (L2 hit rate 27% "
+                               "in the capture): bound by their latency, neither this bandwidth "
+                               "nor the FP32 pipe is saturated"}
     roof["traffic_floor"] = float(np.mean(timed_counts)) * (4 * 8 + 5 * 8 + 4 + 4 + 1)
     status = np.bincount(stat_b, minlength=4)
     return {

@@ -215,9 +215,11 @@ typedef struct mr_batch_config {
                           accelerator and moved to where most of its rays are
                           (one scenario with its current gridded on the
                           bathymetry's grid only);
-                          MR_STAGING_AHEAD from registers loaded a step ahead
-                          with the cell the ray is heading into (every
-                          scenario's current gridded on its bathymetry's grid).
+                          MR_STAGING_AHEAD from the lane's slot of shared
+                          memory, into which the records of the cell the ray
+                          is heading into are copied (cp.async) a step ahead
+                          (every scenario's current gridded on its
+                          bathymetry's grid).
                           Other combinations: MR_ERR_INVALID_ARGUMENT.  One ray
                           per lane. */
 } mr_batch_config;

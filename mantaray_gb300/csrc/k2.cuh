@@ -133,14 +133,14 @@ struct CellCache {
   float4 c0, c1, c2;      // u's and v's coefficients, the current's gradients
 };
 
-// The records of the cell a lane's ray is heading into (the ahead build),
-// loaded a step before the ray enters it.
+// The cell a lane's ray is heading into (the ahead build): its records are
+// copied a step before the ray enters it into the lane's 80-byte slot of
+// shared memory (5 float4: bathymetry 2, current 3).
 struct NextCell {
-  int key;                // cell index held, -1: none
-  float4 b0;
-  float bx, by;
-  float4 c0, c1, c2;
+  int key;                // cell index copied (or in flight), -1: none
 };
+
+extern __shared__ __align__(128) float4 k2_ahead_smem[];
 
 struct RayLane {
   int64_t ray;      // -1: empty slot, -2: no work left
@@ -232,19 +232,36 @@ __device__ __forceinline__ void load_same_grid_cell(const ScenarioDev &s, CellCa
   }
 }
 
+// The ahead build's copies: cp.async (asynchronous global -> shared copies,
+// 16 bytes each, cached in L2 only), committed as one group per cell; a lane
+// waits only for its own groups.
+__device__ __forceinline__ void cp_async16(uint32_t dst, const float4 *src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+}
+
 // The records of cell cb of both fields (modes 2 and 3, the ahead build),
-// unless the lane holds them: from the registers loaded ahead when the ray
-// entered the cell it was predicted to enter.
+// unless the lane holds them: from its shared-memory slot when the ray
+// entered the cell it was predicted to enter (after waiting for the copy,
+// issued a step or more earlier), else from global memory.
 __device__ __forceinline__ void load_same_grid_cell_ahead(const ScenarioDev &s, CellCache &C,
                                                           const NextCell &N, int cb) {
   if (cb != C.bkey) {
     if (cb == N.key) {
-      C.b0 = N.b0;
-      C.bx = N.bx;
-      C.by = N.by;
-      C.c0 = N.c0;
-      C.c1 = N.c1;
-      C.c2 = N.c2;
+      cp_async_wait_all();
+      const float4 *slot = k2_ahead_smem + threadIdx.x * 5;
+      C.b0 = slot[0];
+      const float4 b1 = slot[1];
+      C.bx = b1.x;
+      C.by = b1.y;
+      C.c0 = slot[2];
+      C.c1 = slot[3];
+      C.c2 = slot[4];
       C.bkey = cb;
     } else {
       load_same_grid_cell(s, C, cb);
@@ -254,9 +271,10 @@ __device__ __forceinline__ void load_same_grid_cell_ahead(const ScenarioDev &s, 
 
 // The ahead build's prediction, once a step after the first stage: the
 // neighbour cell the ray leaves its cell into at velocity (vx, vy) (the
-// nearer of its x and y exits), whose records are loaded into L.next now;
-// they are first read when the ray enters that cell, a step or more later,
-// so the load's latency passes while the lane computes.
+// nearer of its x and y exits), whose records are copied into the lane's
+// shared-memory slot now; they are first read when the ray enters that
+// cell, a step or more later, so the copy's latency passes while the lane
+// computes.
 template <int MODE>
 __device__ __forceinline__ void load_ahead(const ScenarioDev &s, RayLane &L, float vx, float vy) {
   int cb, ix, iy;
@@ -278,13 +296,17 @@ __device__ __forceinline__ void load_ahead(const ScenarioDev &s, RayLane &L, flo
   const int key = nj * (s.bathy.nx - 1) + ni;
   NextCell &N = L.next;
   if (key == N.key || key == L.cache.bkey) return;
-  N.b0 = __ldg(s.bathy.cells + static_cast<int64_t>(key) * 2);
-  const float4 b1 = __ldg(s.bathy.cells + static_cast<int64_t>(key) * 2 + 1);
-  N.bx = b1.x;
-  N.by = b1.y;
-  N.c0 = __ldg(s.current.cells + static_cast<int64_t>(key) * 3);
-  N.c1 = __ldg(s.current.cells + static_cast<int64_t>(key) * 3 + 1);
-  N.c2 = __ldg(s.current.cells + static_cast<int64_t>(key) * 3 + 2);
+  cp_async_wait_all();  // the slot's previous copy has landed before it is overwritten
+  const uint32_t slot = static_cast<uint32_t>(__cvta_generic_to_shared(k2_ahead_smem)) +
+                        threadIdx.x * 80u;
+  const float4 *b = s.bathy.cells + static_cast<int64_t>(key) * 2;
+  const float4 *c = s.current.cells + static_cast<int64_t>(key) * 3;
+  cp_async16(slot, b);
+  cp_async16(slot + 16, b + 1);
+  cp_async16(slot + 32, c);
+  cp_async16(slot + 48, c + 1);
+  cp_async16(slot + 64, c + 2);
+  cp_async_commit();
   N.key = key;
 }
 
@@ -710,6 +732,7 @@ __device__ __forceinline__ void k2_body(const BatchArgs &a) {
     }
   }
   if (STAGE == 1) tile_finish(W);
+  if (STAGE == 2) cp_async_wait_all();  // no copy lands after the block has left
 }
 
 // One ray per lane, two builds.  rk4_f32_kernel_1 takes the compiler's
@@ -745,7 +768,8 @@ __global__ void __launch_bounds__(256) rk4_f32_kernel_1t(const __grid_constant__
   k2_body<1, MODE, 1>(a);
 }
 // The ahead build (modes 2 and 3): one ray per lane, with the records of the
-// cell each ray heads into loaded a step early (20 more registers a lane).
+// cell each ray heads into copied a step early into the lane's 80-byte slot
+// of dynamic shared memory.
 template <int MODE>
 __global__ void __launch_bounds__(256) rk4_f32_kernel_1a(BatchArgs a) { k2_body<1, MODE, 2>(a); }
 

@@ -208,8 +208,9 @@ cudaError_t launch_rk4_f32(const BatchArgs &a, int block, int blocks_per_sm, int
   const void *fn = rk4_f32_function(rays_per_lane, block, blocks_per_sm, a.n_scenarios,
                                     a.all_same_grid, a.staging);
   if (!fn) return cudaErrorInvalidValue;
-  return cudaLaunchKernel(fn, dim3(grid), dim3(block), args,
-                          a.staging == 1 ? rk4_f32_tile_smem(block) : 0, stream);
+  const size_t smem = a.staging == 1 ? rk4_f32_tile_smem(block)
+                      : a.staging == 2 ? static_cast<size_t>(block) * 80 : 0;
+  return cudaLaunchKernel(fn, dim3(grid), dim3(block), args, smem, stream);
 }
 
 }  // namespace mr
