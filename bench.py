@@ -43,8 +43,8 @@ GRID_BYTES_PER_RAY_STEP = 4 * 3 * 4 * 8
 OUT_BYTES_PER_ROW = 5 * 8
 # FP32 floating-point operations one ray-step of the batched kernel executes
 # (FADD/FMUL = 1, FFMA = 2), counted by ncu on the 4,096^2 shelf-slope case
-# with the current on the bathymetry's grid.
-FP32_FLOP_PER_RAY_STEP = 432.2
+# with the current on the bathymetry's grid (92.0 FFMA, 36.0 FADD, 36.1 FMUL).
+FP32_FLOP_PER_RAY_STEP = 256.2
 # Algorithmic work of one ray-step (the reference's arithmetic, hand count from
 # src/wave_ray_path.rs:118-216 plus the RK4 update): ~55 FP64 add/mul/div per
 # right-hand side x 4 + ~53 for the update = 270 (36 transcendental calls not
@@ -57,9 +57,9 @@ ALG_FP32_FLOP_PER_RAY_STEP = 710.0
 # DFMA = 2), per right-hand-side arithmetic, counted by ncu on the plain
 # kernel over the seamount workload (65,536 rays x 100 steps)
 # (sm__sass_thread_inst_executed_op_d{add,mul,fma}_pred_on).
-FP64_FLOP_PER_RAY_STEP = {"libm": 1401.4, "identity": 343.6}
+FP64_FLOP_PER_RAY_STEP = {"libm": 1401.4, "identity": 219.3}
 # FP64-pipe instructions per ray-step (sm__inst_executed_pipe_fp64 x 32, same captures)
-FP64_PIPE_INST_PER_RAY_STEP = {"libm": 945.2, "identity": 283.6}
+FP64_PIPE_INST_PER_RAY_STEP = {"libm": 945.2, "identity": 195.4}
 # DRAM bytes (read + written) per ray-step of the plain kernel on the seamount
 # workload: ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch
 # over its 65,536 rays x 1,000 steps (55.5 MB read, 2,573.7 MB written: the
