@@ -592,6 +592,16 @@ def last_finite_states(traj, nr):
     return traj[:, last, idx].cpu().numpy(), last.cpu().numpy()
 
 
+def batch_kernels_per_call(cfg, max_cells: int, n_scenarios: int, decimation: int) -> int:
+    """This project's kernels in one batched call: rk4_f32, the NaN fill of
+    the decimated rows, and with ordering order_keys + 3 per 8-bit pass of the
+    sort key (direction 8 bits, Morton code 2 x cell bits, scenario bits)."""
+    cbits = int(np.ceil(np.log2(max_cells))) if max_cells > 1 else 0
+    sbits = int(np.ceil(np.log2(n_scenarios))) if n_scenarios > 1 else 0
+    passes = (8 + 2 * min(cbits, 16) + sbits + 7) // 8
+    return 1 + (1 if decimation else 0) + ((1 + 3 * passes) if cfg.order else 0)
+
+
 def north_star_batched(args, dev, stream, flush) -> dict:
     """The large single-scenario throughput case: rays entering an 8,192^2
     shelf-slope field at 50 m (h, u, v and their cell gradients as FP32 cell
@@ -749,7 +759,7 @@ def north_star_batched(args, dev, stream, flush) -> dict:
             "rel_position_p99": float(np.nanpercentile(sens, 99)),
             "rel_position_max": float(np.nanmax(sens))},
         "roofline": roof, "clocks": clock,
-        "gpu_launches": args.ns_calls,
+        "gpu_launches": args.ns_calls * batch_kernels_per_call(cfg, args.ns_grid - 1, 1, 0),
     }
 
 
@@ -912,14 +922,8 @@ def batched_arm(args, rank: int, world: int, local_rank: int):
                          out=out, stream=stream)
             return n_all
 
-    # this project's kernels per call: rk4_f32, the NaN fill of the decimated
-    # rows, and with ordering order_keys + 3 per 8-bit pass of the sort key
-    # (direction 8 bits, Morton code 2 x cell bits, scenario bits)
     cmax = max(max(fs[2].shape) - 1 for fs in fields)
-    cbits = int(np.ceil(np.log2(cmax))) if cmax > 1 else 0
-    sbits = int(np.ceil(np.log2(len(handles)))) if len(handles) > 1 else 0
-    passes = (8 + 2 * min(cbits, 16) + sbits + 7) // 8
-    kernels_per_call = 1 + (1 if decimation else 0) + ((1 + 3 * passes) if cfg.order else 0)
+    kernels_per_call = batch_kernels_per_call(cfg, cmax, len(handles), decimation)
     for i in range(args.warmup):
         one(i)
     torch.cuda.synchronize()
