@@ -108,7 +108,7 @@ def parse():
     p.add_argument("--no-autotune", action="store_true")
     p.add_argument("--launch", default=None,
                    help="batched form: fixed launch shape 'block,blocks_per_sm,rays_per_lane,"
-                        "order[,staging]' instead of the autotuner's")
+                        "order[,staging[,sweep_steps]]' instead of the autotuner's")
     # the target measurements reported beside the plain form's line
     p.add_argument("--no-north-star", action="store_true",
                    help="plain form: skip the shelf-slope batched-vs-plain and adjoint-vs-"
@@ -631,14 +631,17 @@ def north_star_batched(args, dev, stream, flush) -> dict:
             f"{steps}steps_graph_replay")
     probe = min(cap, 1 << 20)
     if args.launch:
-        blk, bps, rpl, order, *stg = (int(v) for v in args.launch.split(","))
-        cfg = make_config(blk, bps, rpl, 32, order, stg[0] if stg else 0)
+        blk, bps, rpl, order, *more = (int(v) for v in args.launch.split(","))
+        cfg = make_config(blk, bps, rpl, 32, order, *more[:2])
     else:
-        # short probe for every shape, then the fastest six again over a
-        # long trace, where the rays have spread over the whole field
-        cfg = tracer.autotune(*[t[:probe] for t in ins], dt, min(steps, 1000), t0=t0,
-                              cache_key=f"{torch.cuda.get_device_name(dev)}:{name}:{probe}",
-                              long_steps=min(steps, 10000), long_rays=probe, finalists=6)
+        # short probe of every shape on 2^20 rays, then the fastest six
+        # (and the ordered ones in sweeps) again on 2^22 rays over a long
+        # trace, where the rays have spread over the whole field
+        many = min(cap, 1 << 22)
+        cfg = tracer.autotune(*[t[:many] for t in ins], dt, min(steps, 1000), t0=t0,
+                              cache_key=f"{torch.cuda.get_device_name(dev)}:{name}:{probe}:{many}",
+                              long_steps=min(steps, 10000), long_rays=many, finalists=6,
+                              probe_rays=probe)
     g = tracer.graph(*ins, dt, steps, t0=t0, config=cfg)
     out = g.out
     counts = np.random.default_rng(4004).integers(nominal // 2, cap + 1,
@@ -893,14 +896,19 @@ def batched_arm(args, rank: int, world: int, local_rank: int):
     cfg = default_config()
     tuned = None
     if args.launch:
-        blk, bps, rpl, order, *stg = (int(v) for v in args.launch.split(","))
-        cfg = make_config(blk, bps, rpl, 32, order, stg[0] if stg else 0)
+        blk, bps, rpl, order, *more = (int(v) for v in args.launch.split(","))
+        cfg = make_config(blk, bps, rpl, 32, order, *more[:2])
     elif not args.no_autotune:
         probe = min(n_all, 1 << 20)
-        pin = [t[:probe] for t in ins]
+        # long horizons: the fastest shapes (and the ordered ones in sweeps)
+        # again on 2^22 rays over 10,000 steps, where the rays have spread
+        many = min(n_all, 1 << 22) if steps >= 5000 else probe
+        pin = [t[:many] for t in ins]
         cfg = tracer.autotune(*pin, dt, min(steps, 1000), t0=t0,
-                              scenario=sid[:probe] if sid is not None else None,
-                              cache_key=f"{torch.cuda.get_device_name(dev)}:{name}:{probe}")
+                              scenario=sid[:many] if sid is not None else None,
+                              cache_key=f"{torch.cuda.get_device_name(dev)}:{name}:{probe}:{many}",
+                              long_steps=min(steps, 10000) if steps >= 5000 else None,
+                              long_rays=many, finalists=6, probe_rays=probe)
         tuned = cfg.as_dict()
 
     rng = np.random.default_rng(7)

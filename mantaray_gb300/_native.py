@@ -66,7 +66,8 @@ class BatchConfig(ctypes.Structure):
 
     _fields_ = [("block", ctypes.c_int), ("blocks_per_sm", ctypes.c_int),
                 ("rays_per_lane", ctypes.c_int), ("rebase_interval", ctypes.c_int),
-                ("order", ctypes.c_int), ("staging", ctypes.c_int)]
+                ("order", ctypes.c_int), ("staging", ctypes.c_int),
+                ("sweep_steps", ctypes.c_int)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}

@@ -33,8 +33,9 @@ def default_config() -> N.BatchConfig:
 
 
 def make_config(block=128, blocks_per_sm=4, rays_per_lane=1, rebase_interval=32,
-                order=0, staging=0) -> N.BatchConfig:
-    return N.BatchConfig(block, blocks_per_sm, rays_per_lane, rebase_interval, order, staging)
+                order=0, staging=0, sweep_steps=0) -> N.BatchConfig:
+    return N.BatchConfig(block, blocks_per_sm, rays_per_lane, rebase_interval, order, staging,
+                         sweep_steps)
 
 
 @dataclass
@@ -136,15 +137,20 @@ class BatchTracer:
 
     def autotune(self, x0, y0, kx0, ky0, dt, probe_steps, t0=0.0, scenario=None,
                  candidates=None, repeats=2, cache_key=None, long_steps=None,
-                 long_rays=None, finalists=4) -> N.BatchConfig:
-        """Times every candidate launch shape on a probe run (the given rays
-        for `probe_steps` steps, endpoints only) and returns the fastest.
+                 long_rays=None, finalists=4, sweeps=(128, 256),
+                 probe_rays=None) -> N.BatchConfig:
+        """Times every candidate launch shape on a probe run (the first
+        `probe_rays` of the given rays, default all, for `probe_steps` steps,
+        endpoints only) and returns the fastest.
         With `long_steps`, the `finalists` fastest are timed again on the
         first `long_rays` rays for `long_steps` steps, once each, and the
         fastest of that run wins: a short probe keeps the rays near their
         starts, where the fields they read may fit in L2, while a long trace
-        spreads them over the whole field.  Results are cached in memory and
-        in $MANTARAY_TUNE_CACHE (a JSON file) when that is set."""
+        spreads them over the whole field.  There each ordered one-ray
+        finalist (and the fastest such candidate, if no finalist is one) is
+        also timed in sweeps of each length in `sweeps`, a form that only
+        pays once the rays have spread.  Results are cached in memory and in
+        $MANTARAY_TUNE_CACHE (a JSON file) when that is set."""
         torch = _torch()
         key = cache_key
         cache_path = os.environ.get("MANTARAY_TUNE_CACHE")
@@ -187,16 +193,27 @@ class BatchTracer:
         def sc(rays):
             return None if scenario is None else scenario[: rays[0].numel()]
 
-        rays = (x0, y0, kx0, ky0)
-        out = self.alloc(int(x0.numel()), probe_steps, 0, device=x0.device)
+        p = int(min(x0.numel(), probe_rays or x0.numel()))
+        rays = tuple(t[:p] for t in (x0, y0, kx0, ky0))
+        out = self.alloc(p, probe_steps, 0, device=x0.device)
         ranked = sorted((timed(cfg, rays, probe_steps, repeats, out), i)
                         for i, cfg in enumerate(candidates))
         best = candidates[ranked[0][1]]
         if long_steps:
             m = int(min(x0.numel(), long_rays or x0.numel()))
-            rays = tuple(t[:m] for t in rays)
+            rays = tuple(t[:m] for t in (x0, y0, kx0, ky0))
             out = self.alloc(m, long_steps, 0, device=x0.device)
             finals = [candidates[i] for _, i in ranked[:finalists]]
+
+            def sweepable(c):
+                return c.order == 1 and c.rays_per_lane == 1 and c.staging == 0 and \
+                    c.sweep_steps == 0
+
+            bases = [c for c in finals if sweepable(c)]
+            if not bases:
+                bases = [candidates[i] for _, i in ranked if sweepable(candidates[i])][:1]
+            finals += [make_config(**dict(c.as_dict(), sweep_steps=sw))
+                       for c in bases for sw in sweeps if 0 < sw < long_steps]
             best = min(finals, key=lambda cfg: timed(cfg, rays, long_steps, 1, out))
         if key:
             _TUNE_CACHE[key] = best.as_dict()

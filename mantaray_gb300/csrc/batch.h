@@ -56,6 +56,16 @@ constexpr int kTileCells = 8;
 constexpr int kTileBathyBytes = kTileCells * kTileCells * 2 * 16;
 constexpr int kTileBytes = kTileCells * kTileCells * 5 * 16;
 
+// A running ray between two sweeps of the sweep form: the lane state that
+// carries from one step to the next (the rest -- grid positions of the
+// origin, cell records -- follows from it), 64 bytes.
+struct __align__(16) SweepRay {
+  double ox, oy;                 // FP64 origin
+  float px, py, kx, ky;          // offsets and wavenumber
+  float cpx, cpy, ckx, cky;      // Kahan compensations
+  int32_t step, saved, to_save, to_rebase;
+};
+
 struct BatchArgs {
   // tensor maps of scenario 0's cell records (the tile build): bathymetry
   // [ny-1][nx-1][8 floats], current [ny-1][nx-1][12 floats]
@@ -84,6 +94,17 @@ struct BatchArgs {
   uint8_t *status;           // [n] BatchStatus
   unsigned long long *queue; // work-queue head (scratch, zeroed before the launch)
   const uint32_t *order;     // [n] ray taken at each queue slot, or null (slot = ray)
+  // The sweep form (sweep_steps > 0): a launch advances each ray it takes by
+  // at most sweep_steps steps; a ray still running then leaves its state in
+  // sweep[ray] and its index in next_list[*next_count] for the next launch.
+  // Every launch takes *n_dev rays in the order `order` (the first: the
+  // call's n rays; the later ones: the list, re-ordered).
+  int32_t sweep_steps;
+  int32_t sweep_first;             // 1: the call's first launch (rays from x0, y0, kx0, ky0)
+  SweepRay *sweep;                 // [n_stride]
+  uint32_t *next_list;             // [n_stride]
+  unsigned long long *next_count;
+  const int64_t *n_dev;
 };
 
 // Spatial ordering of the rays (order.cu): keys [2][n_max] and values
@@ -101,6 +122,11 @@ struct OrderArgs {
   uint32_t *counts;
   int tiles;                 // ceil(capacity / kOrderTile)
   int scen_shift;            // bit position of the scenario in the key
+  // the sweep form: order the *n_dev rays list[0 .. *n_dev) by the cell and
+  // direction of their current state in sweep[] (null: the n rays by their
+  // initial states)
+  const uint32_t *list;
+  const SweepRay *sweep;
 };
 
 }  // namespace mr

@@ -28,6 +28,7 @@ struct mr_batch_graph {
   mr::OrderArgs oargs{};
   mr_order_buffers ord;                    // the graph's own ordering scratch
   size_t n_max = 0;
+  bool sweep = false;                      // the sweep form: every launch reads n from the device
 };
 
 namespace {
@@ -141,7 +142,28 @@ int encode_cells(CUtensorMap *m, const float4 *cells, int nx, int ny, int floats
 
 void order_free(mr_order_buffers *o) {
   if (o->mem) cudaFree(o->mem);
+  if (o->sweep_mem) cudaFree(o->sweep_mem);
   *o = mr_order_buffers();
+}
+
+// Makes the sweep scratch hold at least n rays (the ordering scratch is
+// reserved separately; cudaFree waits for work that still uses the old one).
+cudaError_t sweep_reserve(mr_order_buffers *o, size_t n) {
+  if (n <= o->sweep_cap && o->sweep_mem) return cudaSuccess;
+  if (o->sweep_mem) cudaFree(o->sweep_mem);
+  o->sweep_mem = nullptr;
+  o->sweep_cap = 0;
+  auto up = [](size_t v) { return (v + 255) & ~static_cast<size_t>(255); };
+  const size_t states = up(n * sizeof(mr::SweepRay));
+  char *p = nullptr;
+  cudaError_t e = cudaMalloc(reinterpret_cast<void **>(&p), 256 + states + up(n * sizeof(uint32_t)));
+  if (e != cudaSuccess) return e;
+  o->sweep_mem = p;
+  o->sweep_cap = n;
+  o->count = reinterpret_cast<unsigned long long *>(p);
+  o->sweep = reinterpret_cast<mr::SweepRay *>(p + 256);
+  o->list = reinterpret_cast<uint32_t *>(p + 256 + states);
+  return cudaSuccess;
 }
 
 // Makes the ordering scratch hold at least n rays (the old contents are not
@@ -200,6 +222,10 @@ int check_config(const mr_batch_config *cfg) {
     return fail(MR_ERR_INVALID_ARGUMENT, "staging must be 0, 1 or 2");
   if (cfg->staging && cfg->rays_per_lane != 1)
     return fail(MR_ERR_INVALID_ARGUMENT, "staging traces one ray per lane");
+  if (cfg->sweep_steps < 0) return fail(MR_ERR_INVALID_ARGUMENT, "sweep_steps must be >= 0");
+  if (cfg->sweep_steps > 0 && (cfg->order != 1 || cfg->rays_per_lane != 1 || cfg->staging))
+    return fail(MR_ERR_INVALID_ARGUMENT,
+                "sweeps need order = 1, one ray per lane and no staging");
   return MR_OK;
 }
 
@@ -288,22 +314,52 @@ int fill_args(mr_batch *b, size_t n, size_t n_stride, const uint8_t *ray_scenari
 // Stream work of one batched call: reset the queue, NaN-fill the saved rows
 // (rows a ray does not reach stay NaN, as the reference pads them), order
 // the rays when cfg->order (into `ord`, sized for n_stride rays), launch.
-cudaError_t enqueue(const mr_batch *b, mr::BatchArgs a, const mr_batch_config *cfg,
+// The sweep form launches ceil(max_steps / sweep_steps) times (at least
+// once), the running rays listed, counted and re-ordered between launches,
+// all on the stream: the host never waits.  *a gets the arguments of the
+// (first) launch.
+cudaError_t enqueue(const mr_batch *b, mr::BatchArgs *a, const mr_batch_config *cfg,
                     const mr_order_buffers *ord, cudaStream_t s) {
-  cudaError_t e = cudaMemsetAsync(a.queue, 0, sizeof(unsigned long long), s);
+  cudaError_t e = cudaMemsetAsync(a->queue, 0, sizeof(unsigned long long), s);
   if (e != cudaSuccess) return e;
-  if (a.decimation > 0 && a.save_cap > 0) {
-    e = mr::launch_fill_nan(a.saved, 5 * a.save_cap * a.n_stride, s);
+  if (a->decimation > 0 && a->save_cap > 0) {
+    e = mr::launch_fill_nan(a->saved, 5 * a->save_cap * a->n_stride, s);
     if (e != cudaSuccess) return e;
   }
-  a.order = nullptr;
+  a->order = nullptr;
+  mr::OrderArgs o{};
   if (cfg->order) {
-    const mr::OrderArgs o = order_args(b, a, *ord);
-    e = mr::launch_order(o, a.n_stride, b->order_passes, s);
+    o = order_args(b, *a, *ord);
+    e = mr::launch_order(o, a->n_stride, b->order_passes, s);
     if (e != cudaSuccess) return e;
-    a.order = ord->vals[b->order_passes & 1];
+    a->order = ord->vals[b->order_passes & 1];
   }
-  return mr::launch_rk4_f32(a, cfg->block, cfg->blocks_per_sm, cfg->rays_per_lane, s);
+  if (cfg->sweep_steps <= 0)
+    return mr::launch_rk4_f32(*a, cfg->block, cfg->blocks_per_sm, cfg->rays_per_lane, s);
+  e = cudaMemsetAsync(ord->count, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return e;
+  a->sweep_steps = cfg->sweep_steps;
+  a->sweep_first = 1;
+  a->sweep = ord->sweep;
+  a->next_list = ord->list;
+  a->next_count = ord->count;
+  a->n_dev = ord->n_dev;
+  e = mr::launch_rk4_f32(*a, cfg->block, cfg->blocks_per_sm, cfg->rays_per_lane, s);
+  if (e != cudaSuccess) return e;
+  mr::BatchArgs later = *a;
+  later.sweep_first = 0;
+  mr::OrderArgs ol = o;
+  ol.list = ord->list;
+  ol.sweep = ord->sweep;
+  const int64_t sweeps = (a->max_steps + cfg->sweep_steps - 1) / cfg->sweep_steps;
+  for (int64_t k = 1; k < sweeps; ++k) {
+    e = mr::launch_sweep_next(ord->n_dev, ord->count, a->queue, s);
+    if (e == cudaSuccess) e = mr::launch_order(ol, a->n_stride, b->order_passes, s);
+    if (e == cudaSuccess)
+      e = mr::launch_rk4_f32(later, cfg->block, cfg->blocks_per_sm, cfg->rays_per_lane, s);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 }  // namespace
@@ -431,11 +487,13 @@ int mr_batch_trace_device(mr_batch *b, size_t n, const uint8_t *ray_scenario, co
   cudaError_t e = cudaSuccess;
   if (cfg->order) {
     // the scratch may be in use by earlier calls on this stream: order them first
-    if (n > b->ord.cap) e = cudaStreamSynchronize(s);
+    if (n > b->ord.cap || (cfg->sweep_steps > 0 && n > b->ord.sweep_cap))
+      e = cudaStreamSynchronize(s);
     if (e == cudaSuccess) e = order_reserve(&b->ord, n);
+    if (e == cudaSuccess && cfg->sweep_steps > 0) e = sweep_reserve(&b->ord, n);
     if (e != cudaSuccess) return cuda_fail(e, "ordering scratch");
   }
-  e = enqueue(b, a, cfg, &b->ord, s);
+  e = enqueue(b, &a, cfg, &b->ord, s);
   if (e != cudaSuccess) return cuda_fail(e, "rk4_f32 launch");
   return MR_OK;
 }
@@ -460,18 +518,23 @@ int mr_batch_graph_create(mr_batch *b, size_t n_max, const uint8_t *ray_scenario
   gr->n_max = n_max;
   cudaStream_t s = nullptr;
   cudaError_t e = cudaSuccess;
+  gr->sweep = cfg->sweep_steps > 0;
   if (cfg->order) {
     e = order_reserve(&gr->ord, n_max);
+    if (e == cudaSuccess && gr->sweep) e = sweep_reserve(&gr->ord, n_max);
     gr->oargs = order_args(b, a, gr->ord);
   }
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
   // the integrator build for this shape, chosen (an occupancy query) before
   // the capture begins
-  (void)mr::rk4_f32_function(cfg->rays_per_lane, cfg->block, cfg->blocks_per_sm,
-                             b->n_scenarios, all_same_grid(b), cfg->staging);
+  const void *k2 = mr::rk4_f32_function(cfg->rays_per_lane, cfg->block, cfg->blocks_per_sm,
+                                        b->n_scenarios, all_same_grid(b), cfg->staging,
+                                        gr->sweep);
   if (e == cudaSuccess) e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
-    cudaError_t le = enqueue(b, a, cfg, &gr->ord, s);
+    // the kernel node's arguments as captured (queue order included), for
+    // the launches that change n
+    cudaError_t le = enqueue(b, &gr->args, cfg, &gr->ord, s);
     e = cudaStreamEndCapture(s, &gr->graph);
     if (le != cudaSuccess) e = le;
   }
@@ -487,12 +550,13 @@ int mr_batch_graph_create(mr_batch *b, size_t n_max, const uint8_t *ray_scenario
       cudaKernelNodeParams p{};
       e = cudaGraphKernelNodeGetParams(nodes[i], &p);
       if (e != cudaSuccess) break;
-      if (p.func == mr::order_keys_function()) {
+      // the ordering of the call's rays (a sweep form's later orderings
+      // take their rays from the list and n from the device)
+      if (p.func == mr::order_keys_function() &&
+          static_cast<const mr::OrderArgs *>(p.kernelParams[0])->list == nullptr) {
         gr->order_node = nodes[i];
         gr->order_params = p;
-      } else if (p.func == mr::rk4_f32_function(cfg->rays_per_lane, cfg->block,
-                                                cfg->blocks_per_sm, b->n_scenarios,
-                                                all_same_grid(b), cfg->staging)) {
+      } else if (p.func == k2 && !gr->kernel_node) {
         gr->kernel_node = nodes[i];
         gr->params = p;
       }
@@ -516,12 +580,15 @@ int mr_batch_graph_launch(mr_batch_graph *gr, size_t n, void *stream) {
   if (!g.ok()) return fail(MR_ERR_CUDA, "cannot select the batch's device");
   // n is a kernel argument: the executable graph's kernel node takes the new
   // value for this and later launches (launches already queued keep theirs).
+  // (The sweep form's launches read n from the device, where the first
+  // ordering kernel puts it.)
   gr->args.n = static_cast<int64_t>(n);
   void *kargs[1] = {&gr->args};
   cudaKernelNodeParams p = gr->params;
   p.kernelParams = kargs;
   p.extra = nullptr;
-  cudaError_t e = cudaGraphExecKernelNodeSetParams(gr->exec, gr->kernel_node, &p);
+  cudaError_t e = cudaSuccess;
+  if (!gr->sweep) e = cudaGraphExecKernelNodeSetParams(gr->exec, gr->kernel_node, &p);
   if (e == cudaSuccess && gr->order_node) {
     gr->oargs.n = static_cast<int64_t>(n);
     void *oargs[1] = {&gr->oargs};

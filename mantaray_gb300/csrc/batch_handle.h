@@ -9,7 +9,9 @@
 
 // Device scratch of the spatial ordering (order.cu) for up to `cap` rays:
 // one allocation holding n_dev, keys [2][cap], vals [2][cap], counts
-// [256][tiles].
+// [256][tiles]; and for the sweep form, for up to `sweep_cap` rays, another
+// holding the list counter, the running rays' states [sweep_cap] and the
+// list [sweep_cap].
 struct mr_order_buffers {
   void *mem = nullptr;
   size_t cap = 0;
@@ -18,6 +20,11 @@ struct mr_order_buffers {
   uint64_t *keys[2] = {nullptr, nullptr};
   uint32_t *vals[2] = {nullptr, nullptr};
   uint32_t *counts = nullptr;
+  void *sweep_mem = nullptr;
+  size_t sweep_cap = 0;
+  unsigned long long *count = nullptr;
+  mr::SweepRay *sweep = nullptr;
+  uint32_t *list = nullptr;
 };
 
 struct mr_batch {

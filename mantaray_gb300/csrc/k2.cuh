@@ -153,6 +153,7 @@ struct RayLane {
   int32_t saved;
   int32_t to_save;    // steps until the next decimated row (no 64-bit modulo per step)
   int32_t to_rebase;  // steps until the next origin rebase
+  int32_t limit;      // the sweep form: the step at which the ray leaves this launch
   CellCache cache;
   NextCell next;      // the ahead build only
 };
@@ -590,6 +591,43 @@ __device__ __forceinline__ void start(const BatchArgs &a, RayLane &L, int64_t r)
   }
 }
 
+// The sweep form: a ray taken up again from the state a previous launch left,
+// with no cell held -- exactly the lane of a launch
+// that traced it without stopping, as the cell records are a cache of
+// immutable values and the origin's grid positions a function of the origin.
+template <int MODE>
+__device__ __forceinline__ void resume(const BatchArgs &a, RayLane &L, int64_t r) {
+  L.ray = r;
+  L.scen = ((MODE == 0 || MODE == 3) && a.ray_scenario) ? static_cast<int>(a.ray_scenario[r])
+                                                         : 0;
+  if (L.scen >= a.n_scenarios) L.scen = 0;
+  const ScenarioDev &s = scenario<MODE>(a, L.scen);
+  const float4 *p = reinterpret_cast<const float4 *>(a.sweep + r);
+  const double2 o = *reinterpret_cast<const double2 *>(p);
+  const float4 q = p[1], c = p[2];
+  const int4 k = *reinterpret_cast<const int4 *>(p + 3);
+  L.ox = o.x; L.oy = o.y;
+  L.px = q.x; L.py = q.y; L.kx = q.z; L.ky = q.w;
+  L.cpx = c.x; L.cpy = c.y; L.ckx = c.z; L.cky = c.w;
+  L.step = k.x; L.saved = k.y; L.to_save = k.z; L.to_rebase = k.w;
+  L.pb = grid_pos(s.bathy, L.ox, L.oy);
+  L.pc = s.same_grid ? L.pb : grid_pos(s.current, L.ox, L.oy);
+  CellCache &C = L.cache;
+  C.bkey = C.ckey = -1;
+  C.b0 = C.c0 = C.c1 = C.c2 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  C.bx = C.by = 0.0f;
+  const int64_t lim = static_cast<int64_t>(L.step) + a.sweep_steps;
+  L.limit = static_cast<int32_t>(lim < a.max_steps ? lim : a.max_steps);
+}
+
+__device__ __forceinline__ void store_sweep(const BatchArgs &a, const RayLane &L) {
+  float4 *p = reinterpret_cast<float4 *>(a.sweep + L.ray);
+  *reinterpret_cast<double2 *>(p) = make_double2(L.ox, L.oy);
+  p[1] = make_float4(L.px, L.py, L.kx, L.ky);
+  p[2] = make_float4(L.cpx, L.cpy, L.ckx, L.cky);
+  *reinterpret_cast<int4 *>(p + 3) = make_int4(L.step, L.saved, L.to_save, L.to_rebase);
+}
+
 // The status of a step whose four stages did not all succeed: the stages
 // again, in order, up to the first that fails (the same arithmetic on the
 // same inputs, so the same values and the same first failure).  Taken once
@@ -682,11 +720,12 @@ __device__ __forceinline__ void tile_refresh(const BatchArgs &a, const RayLane &
   tile_load(a, W, ti, tj);
 }
 
-template <int RPT, int MODE, int STAGE>
+template <int RPT, int MODE, int STAGE, bool SWEEP = false>
 __device__ __forceinline__ void k2_body(const BatchArgs &a) {
+  static_assert(!SWEEP || (RPT == 1 && STAGE == 0), "the sweep form traces one ray per lane");
   const int lane = threadIdx.x & 31;
   const unsigned lt_mask = (1u << lane) - 1u;
-  const int64_t n = a.n;
+  const int64_t n = SWEEP ? *a.n_dev : a.n;
   const int32_t max_steps = static_cast<int32_t>(a.max_steps);
   RayLane L[RPT];
 #pragma unroll
@@ -695,6 +734,24 @@ __device__ __forceinline__ void k2_body(const BatchArgs &a) {
   if (STAGE == 1) W = tile_init();
   int iter = 0;
   while (true) {
+    if (SWEEP) {
+      // rays at the end of this launch's sweep: state out, listed for the
+      // next launch (one atomic per warp)
+      const bool out = L[0].ray >= 0 && L[0].step >= L[0].limit && L[0].step < max_steps;
+      const unsigned leaving = __ballot_sync(kFull, out);
+      if (leaving) {
+        const int leader = __ffs(leaving) - 1;
+        unsigned long long base = 0;
+        if (lane == leader)
+          base = atomicAdd(a.next_count, static_cast<unsigned long long>(__popc(leaving)));
+        base = __shfl_sync(kFull, base, leader);
+        if (out) {
+          store_sweep(a, L[0]);
+          a.next_list[base + __popc(leaving & lt_mask)] = static_cast<uint32_t>(L[0].ray);
+          L[0].ray = -1;
+        }
+      }
+    }
     // refill empty slots from the work queue, one atomic per warp and slot
 #pragma unroll
     for (int j = 0; j < RPT; ++j) {
@@ -707,7 +764,14 @@ __device__ __forceinline__ void k2_body(const BatchArgs &a) {
         if (L[j].ray == -1) {
           const int64_t r = static_cast<int64_t>(base) + __popc(need & lt_mask);
           if (r < n) {
-            start<MODE>(a, L[j], a.order ? static_cast<int64_t>(__ldg(a.order + r)) : r);
+            const int64_t ray = a.order ? static_cast<int64_t>(__ldg(a.order + r)) : r;
+            if (SWEEP && !a.sweep_first) {
+              resume<MODE>(a, L[j], ray);
+            } else {
+              start<MODE>(a, L[j], ray);
+              if (SWEEP) L[j].limit = a.sweep_steps < a.max_steps ? a.sweep_steps
+                                                                  : static_cast<int32_t>(a.max_steps);
+            }
             if (STAGE == 2) L[j].next.key = -1;
           } else {
             L[j].ray = -2;
@@ -755,6 +819,15 @@ template <int MODE>
 __global__ void __launch_bounds__(256) rk4_f32_kernel_1(BatchArgs a) { k2_body<1, MODE, 0>(a); }
 template <int MODE>
 __global__ void __maxnreg__(72) rk4_f32_kernel_1r(BatchArgs a) { k2_body<1, MODE, 0>(a); }
+// The sweep form of both: each launch advances its rays by at most
+// sweep_steps steps, the first from their initial states (sweep_first), the
+// later ones from the states the previous launch left.
+template <int MODE>
+__global__ void __launch_bounds__(256) rk4_f32_kernel_1s(BatchArgs a) {
+  k2_body<1, MODE, 0, true>(a);
+}
+template <int MODE>
+__global__ void __maxnreg__(72) rk4_f32_kernel_1rs(BatchArgs a) { k2_body<1, MODE, 0, true>(a); }
 // Two rays per lane hold twice the lane state: no cap.
 template <int MODE>
 __global__ void __launch_bounds__(256) rk4_f32_kernel_2(BatchArgs a) { k2_body<2, MODE, 0>(a); }

@@ -35,15 +35,16 @@ cudaError_t launch_rk4_f32(const BatchArgs &a, int block, int blocks_per_sm, int
                            cudaStream_t stream);
 // The integrator build a launch of this shape runs, for n_scenarios
 // scenarios (same_grid: every scenario's current is gridded on its
-// bathymetry's grid; staging: MR_STAGING_*, null where that build does not
-// exist); a graph's kernel node is found by it.
+// bathymetry's grid; staging: MR_STAGING_*; sweep: the sweep form; null where
+// that build does not exist); a graph's kernel node is found by it.
 const void *rk4_f32_function(int rays_per_lane, int block, int blocks_per_sm, int n_scenarios,
-                             int same_grid, int staging);
+                             int same_grid, int staging, int sweep);
 // Dynamic shared memory of the tile build for blocks of `block` threads.
 size_t rk4_f32_tile_smem(int block);
 // The single-scenario builds (rk4_f32_one.cu): 0 one ray per lane, 1 the same
 // capped at 72 registers, 2 two rays per lane, 3 the tile build, 4 the ahead
-// build (3 and 4: same grid only, else null).
+// build (3 and 4: same grid only, else null), 5 and 6 the sweep form of 0
+// and 1.
 const void *rk4_f32_one_function(int build, int same_grid);
 cudaError_t launch_fill_nan(float *p, int64_t count, cudaStream_t stream);
 
@@ -53,5 +54,9 @@ cudaError_t launch_fill_nan(float *p, int64_t count, cudaStream_t stream);
 int order_tiles(int64_t n_max);
 cudaError_t launch_order(const OrderArgs &o, int64_t n_max, int passes, cudaStream_t stream);
 const void *order_keys_function();
+// Between two sweeps: *n_dev = *next_count, then the list counter and the
+// work-queue head back to zero (one thread).
+cudaError_t launch_sweep_next(int64_t *n_dev, unsigned long long *next_count,
+                              unsigned long long *queue, cudaStream_t stream);
 
 }  // namespace mr

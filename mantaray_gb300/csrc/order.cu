@@ -55,23 +55,56 @@ __device__ __forceinline__ uint32_t cell_coord(double v, double v0, double sp) {
   return c >= 65535.0 ? 65535u : static_cast<uint32_t>(c);
 }
 
-__global__ void order_keys(OrderArgs o) {
-  if (blockIdx.x == 0 && threadIdx.x == 0) *o.n_dev = o.n;
-  const int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (r >= o.n) return;
-  int s = o.ray_scenario ? static_cast<int>(o.ray_scenario[r]) : 0;
+__device__ __forceinline__ uint64_t order_key(const OrderArgs &o, int s, double x, double y,
+                                              float kx, float ky) {
   if (s >= o.n_scenarios) s = 0;  // as the batched kernel maps it
   const PackedGrid &g = o.scen[s].bathy;
-  const uint32_t cx = cell_coord(o.x0[r], g.x0, g.sp_x);
-  const uint32_t cy = cell_coord(o.y0[r], g.y0, g.sp_y);
+  const uint32_t cx = cell_coord(x, g.x0, g.sp_x);
+  const uint32_t cy = cell_coord(y, g.y0, g.sp_y);
   const uint32_t morton = spread16(cx) | (spread16(cy) << 1);
-  const float th = atan2f(static_cast<float>(o.ky0[r]), static_cast<float>(o.kx0[r]));
+  const float th = atan2f(ky, kx);
   float tb = (th + 3.14159265f) * (256.0f / 6.28318531f);
   tb = fminf(fmaxf(tb, 0.0f), 255.0f);  // NaN -> 0
-  const uint64_t key = (static_cast<uint64_t>(s) << o.scen_shift) |
-                       (static_cast<uint64_t>(morton) << 8) | static_cast<uint64_t>(tb);
-  o.keys[0][r] = key;
-  o.vals[0][r] = static_cast<uint32_t>(r);
+  return (static_cast<uint64_t>(s) << o.scen_shift) | (static_cast<uint64_t>(morton) << 8) |
+         static_cast<uint64_t>(tb);
+}
+
+// Grid-stride over the rays (a fixed grid: a sweep's list is usually far
+// shorter than the capacity).  Without a list: the n rays by their initial
+// states, n stored for the later kernels.  With one: the *n_dev listed rays
+// by their current states (position origin + offset, as the batched kernel
+// stores it; wavenumber without its compensation: a key needs no more).
+__global__ void order_keys(OrderArgs o) {
+  int64_t n;
+  if (o.list) {
+    n = *o.n_dev;
+  } else {
+    n = o.n;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *o.n_dev = o.n;
+  }
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    uint32_t ray;
+    double x, y;
+    float kx, ky;
+    if (o.list) {
+      ray = o.list[i];
+      const SweepRay &S = o.sweep[ray];
+      x = S.ox + (static_cast<double>(S.px) - static_cast<double>(S.cpx));
+      y = S.oy + (static_cast<double>(S.py) - static_cast<double>(S.cpy));
+      kx = S.kx;
+      ky = S.ky;
+    } else {
+      ray = static_cast<uint32_t>(i);
+      x = o.x0[i];
+      y = o.y0[i];
+      kx = static_cast<float>(o.kx0[i]);
+      ky = static_cast<float>(o.ky0[i]);
+    }
+    const int s = o.ray_scenario ? static_cast<int>(o.ray_scenario[ray]) : 0;
+    o.keys[0][i] = order_key(o, s, x, y, kx, ky);
+    o.vals[0][i] = ray;
+  }
 }
 
 __global__ void __launch_bounds__(kOrderThreads) order_hist(OrderArgs o, int pass) {
@@ -92,20 +125,28 @@ __global__ void __launch_bounds__(kOrderThreads) order_hist(OrderArgs o, int pas
   o.counts[static_cast<int64_t>(t) * o.tiles + blockIdx.x] = h[t];
 }
 
-// Exclusive scan of counts[0 .. 256 * tiles) in place, by one block in chunks
-// of 4 * kScanThreads.
+// Exclusive scan in place of the digit counts [256][tiles], digit-major, over
+// the tiles that hold rays (the first ceil(n / kOrderTile)), by one block in
+// chunks of 4 * kScanThreads.
 __global__ void __launch_bounds__(kScanThreads) order_scan(OrderArgs o) {
   __shared__ unsigned warp_sum[kScanThreads / 32];
   __shared__ unsigned carry_s;
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-  const int64_t total = 256ll * o.tiles;
+  // only the tiles that hold rays: the counts of the others are never read
+  const int64_t n = *o.n_dev;
+  const int used = static_cast<int>((n + kOrderTile - 1) / kOrderTile);
+  const int64_t total = 256ll * used;
+  auto at = [&](int64_t i) -> uint32_t & {  // i < 256 * used < 2^32
+    const uint32_t u = static_cast<uint32_t>(i), d = u / static_cast<uint32_t>(used);
+    return o.counts[static_cast<int64_t>(d) * o.tiles + (u - d * static_cast<uint32_t>(used))];
+  };
   if (t == 0) carry_s = 0u;
   __syncthreads();
   for (int64_t base = 0; base < total; base += 4ll * kScanThreads) {
     const int64_t i0 = base + 4ll * t;
     unsigned v[4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) v[k] = (i0 + k < total) ? o.counts[i0 + k] : 0u;
+    for (int k = 0; k < 4; ++k) v[k] = (i0 + k < total) ? at(i0 + k) : 0u;
     const unsigned local = v[0] + v[1] + v[2] + v[3];
     unsigned incl = local;  // inclusive scan across the warp
 #pragma unroll
@@ -129,7 +170,7 @@ __global__ void __launch_bounds__(kScanThreads) order_scan(OrderArgs o) {
     unsigned run = carry_s + warp_sum[w] + (incl - local);
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-      if (i0 + k < total) o.counts[i0 + k] = run;
+      if (i0 + k < total) at(i0 + k) = run;
       run += v[k];
     }
     __syncthreads();
@@ -186,7 +227,22 @@ __global__ void __launch_bounds__(kOrderThreads) order_scatter(OrderArgs o, int 
   }
 }
 
+// The rays the last sweep left running become the next sweep's work; the
+// list counter and the work-queue head start again from zero.
+__global__ void sweep_next(int64_t *n_dev, unsigned long long *next_count,
+                           unsigned long long *queue) {
+  *n_dev = static_cast<int64_t>(*next_count);
+  *next_count = 0ull;
+  *queue = 0ull;
+}
+
 }  // namespace
+
+cudaError_t launch_sweep_next(int64_t *n_dev, unsigned long long *next_count,
+                              unsigned long long *queue, cudaStream_t stream) {
+  sweep_next<<<1, 1, 0, stream>>>(n_dev, next_count, queue);
+  return cudaGetLastError();
+}
 
 int order_tiles(int64_t n_max) {
   return static_cast<int>((n_max + kOrderTile - 1) / kOrderTile);
@@ -194,7 +250,12 @@ int order_tiles(int64_t n_max) {
 
 cudaError_t launch_order(const OrderArgs &o, int64_t n_max, int passes, cudaStream_t stream) {
   if (n_max <= 0) return cudaSuccess;
-  const unsigned kgrid = static_cast<unsigned>((n_max + kOrderThreads - 1) / kOrderThreads);
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  const int64_t blocks = (n_max + kOrderThreads - 1) / kOrderThreads;
+  const unsigned kgrid = static_cast<unsigned>(blocks < 8ll * sms ? blocks : 8ll * sms);
   order_keys<<<kgrid, kOrderThreads, 0, stream>>>(o);
   for (int p = 0; p < passes; ++p) {
     order_hist<<<o.tiles, kOrderThreads, 0, stream>>>(o, p);

@@ -104,41 +104,67 @@ struct RhsIdentity {
     // group_velocity's k <= 0 error (h > 0 or NaN): k is >= 0 or NaN here
     if (!(hg[0] <= 0.0f) && (__double_as_longlong(k) << 1) == 0) return RHS_ARGUMENT_OUT_OF_BOUNDS;
     const double a = k * h;
-    // the deep-water form needs finite gradients (a NaN one makes the general
-    // form's refraction term NaN, which stops the ray as in the reference)
-    // and a finite depth
+    const double gk = kG * k;
+    // Deep water, 22 < a < 1e300: exp(-2a) < 8e-20, far below half an ulp
+    // of 1, so -expm1(-2a) rounds to exactly 1: tanh a = 1 and the terms in
+    // exp(-2a) (a / cosh^2 a, the refraction factor f) are exactly 0.  The
+    // range is tested on the bit pattern: for doubles of either sign, NaN
+    // included, signed 64-bit order of the bits gives the same answer as
+    // the two comparisons, on the integer pipe.  The deep-water form also
+    // needs finite gradients (a NaN one makes the refraction term NaN, which
+    // stops the ray as in the reference).
+    const long long ab = __double_as_longlong(a);
     const uint32_t gx = bits_of(hg[1]), gy = bits_of(hg[2]);
-    if (a > 22.0 && a < 1.0e300 && (gx & 0x7f800000u) != 0x7f800000u &&
-        (gy & 0x7f800000u) != 0x7f800000u) {
-      // deep water: exp(-2a) < 8e-20, far below half an ulp of 1, so
-      // -expm1(-2a) rounds to exactly 1: tanh a = 1, and the terms in
-      // exp(-2a) (a / cosh^2 a, the refraction factor f) are exactly 0 in the
-      // general branch too.  c_g and the current's terms are the general
-      // branch's bits; the refraction term is dropped rather than added as
-      // a signed zero.
-      const double rs = rsqrt(kG * k);              // 1 / sqrt(g k)
-      const double cg = (kG / 2.0) * rs;            // h > 0 here
+    const bool deep = ab > 0x4036000000000000ll /* 22.0 */ &&
+                      ab < 0x7e37e43c8800759cll /* 1e300 */ &&
+                      (gx & 0x7f800000u) != 0x7f800000u && (gy & 0x7f800000u) != 0x7f800000u;
+    // Deep-water lanes skip the expm1, the reciprocal and the products by
+    // zero.  When every converged lane is in deep water the warp takes the
+    // deep-water form alone; otherwise every operation but those is shared,
+    // so a warp whose rays are in both regimes runs the general form once
+    // rather than both forms.  With tanh a = 1 the shared operations give
+    // the deep-water form's bits (gkt = g k, c_g = (g/2) rs), so a lane's
+    // result does not depend on its neighbours.  The refraction term is
+    // dropped rather than added as a signed zero.
+    if (__all_sync(__activemask(), deep)) {
+      const double rs = rsqrt(gk);                  // 1 / sqrt(g k)
+      const double cg = (kG / 2.0) * rs;
       out[0] = fma(cg, kx * rk, cur[0]);
       out[1] = fma(cg, ky * rk, cur[1]);
       out[2] = -fma(kx, cur[2], ky * cur[4]);
       out[3] = -fma(kx, cur[3], ky * cur[5]);
       return RHS_OK;
     }
-    const double m = -expm1(-2.0 * a);              // 1 - q
-    const double q = 1.0 - m;                       // exp(-2a)
-    const double w = __drcp_rn(m * (2.0 - m));      // 1 / (m (1 + q))
-    const double r = m * w;                         // 1 / (1 + q)
-    const double th = m * r;                        // tanh a
-    const double gkt = (kG * k) * th;
+    double gkt = gk, fac = 1.0, fq = 0.0;
+    if (!deep) {
+      const double m = -expm1(-2.0 * a);            // 1 - q
+      const double q = 1.0 - m;                     // exp(-2a)
+      const double w = __drcp_rn(m * (2.0 - m));    // 1 / (m (1 + q))
+      const double r = m * w;                       // 1 / (1 + q)
+      const double th = m * r;                      // tanh a
+      const double q4 = 4.0 * q;
+      gkt = gk * th;
+      fac = fma(a * q4, r * r, th);                 // tanh a + a / cosh^2 a
+      fq = q4 * w;                                  // 1 / (sinh a cosh a)
+    }
     const double rs = rsqrt(gkt);                   // 1 / sqrt(g k tanh)
-    const double q4 = 4.0 * q;
-    double cg = (kG / 2.0) * (fma(a * q4, r * r, th) * rs);
+    double cgr = rs, f = 0.0;
+    if (!deep) {
+      cgr = fac * rs;
+      f = (-0.5 * k) * (fq * (gkt * rs));
+    }
+    double cg = (kG / 2.0) * cgr;
     if (hg[0] <= 0.0f) cg = f64_nan();
-    const double f = (-0.5 * k) * ((q4 * w) * (gkt * rs));
     out[0] = fma(cg, kx * rk, cur[0]);
     out[1] = fma(cg, ky * rk, cur[1]);
-    out[2] = fma(f, f2d(hg[1]), -fma(kx, cur[2], ky * cur[4]));
-    out[3] = fma(f, f2d(hg[2]), -fma(kx, cur[3], ky * cur[5]));
+    double t2 = -fma(kx, cur[2], ky * cur[4]);
+    double t3 = -fma(kx, cur[3], ky * cur[5]);
+    if (!deep) {
+      t2 = fma(f, f2d(hg[1]), t2);
+      t3 = fma(f, f2d(hg[2]), t3);
+    }
+    out[2] = t2;
+    out[3] = t3;
     return RHS_OK;
   }
 };

@@ -147,28 +147,35 @@ cudaError_t launch_fill_nan(float *p, int64_t count, cudaStream_t stream) {
   return cudaGetLastError();
 }
 
-// The three builds of each table mode: [0] one ray per lane, uncapped; [1]
-// the same capped at 72 registers; [2] two rays per lane.  Row 0: mode 0,
-// row 1: mode 3 (every current on its bathymetry's grid).
-static const void *table_builds[2][3] = {
+// The builds of each table mode: [0] one ray per lane, uncapped; [1] the
+// same capped at 72 registers; [2] two rays per lane; [3] and [4] the sweep
+// form of [0] and [1].  Row 0: mode 0, row 1: mode 3 (every current on its
+// bathymetry's grid).
+static const void *table_builds[2][5] = {
     {reinterpret_cast<const void *>(&rk4_f32_kernel_1<0>),
      reinterpret_cast<const void *>(&rk4_f32_kernel_1r<0>),
-     reinterpret_cast<const void *>(&rk4_f32_kernel_2<0>)},
+     reinterpret_cast<const void *>(&rk4_f32_kernel_2<0>),
+     reinterpret_cast<const void *>(&rk4_f32_kernel_1s<0>),
+     reinterpret_cast<const void *>(&rk4_f32_kernel_1rs<0>)},
     {reinterpret_cast<const void *>(&rk4_f32_kernel_1<3>),
      reinterpret_cast<const void *>(&rk4_f32_kernel_1r<3>),
-     reinterpret_cast<const void *>(&rk4_f32_kernel_2<3>)}};
+     reinterpret_cast<const void *>(&rk4_f32_kernel_2<3>),
+     reinterpret_cast<const void *>(&rk4_f32_kernel_1s<3>),
+     reinterpret_cast<const void *>(&rk4_f32_kernel_1rs<3>)}};
 
-// Resident blocks per SM of each mode's uncapped one-ray build by block
-// size (multiples of 32 up to 256), queried once; 0: not yet known.
-static std::atomic<int> g_resident_1[4][9];
+// Resident blocks per SM of each mode's uncapped one-ray build (plain and
+// sweep form) by block size (multiples of 32 up to 256), queried once; 0:
+// not yet known.
+static std::atomic<int> g_resident_1[2][4][9];
 
 size_t rk4_f32_tile_smem(int block) {
   return static_cast<size_t>(block / 32) * (kTileBytes + 8);
 }
 
 const void *rk4_f32_function(int rays_per_lane, int block, int blocks_per_sm, int n_scenarios,
-                             int same_grid, int staging) {
+                             int same_grid, int staging, int sweep) {
   const int mode = n_scenarios == 1 ? (same_grid ? 2 : 1) : (same_grid ? 3 : 0);
+  if (sweep && (staging != 0 || rays_per_lane != 1)) return nullptr;
   if (staging == 1) return (mode == 2 && rays_per_lane == 1) ? rk4_f32_one_function(3, 1) : nullptr;
   if (staging == 2) {
     if (rays_per_lane != 1) return nullptr;
@@ -176,13 +183,18 @@ const void *rk4_f32_function(int rays_per_lane, int block, int blocks_per_sm, in
     if (mode == 3) return reinterpret_cast<const void *>(&rk4_f32_kernel_1a<3>);
     return nullptr;
   }
+  // [0] uncapped, [1] capped, [2] two rays per lane; the sweep form of [0]
+  // and [1] in their place
+  static const int kOneBuild[2][3] = {{0, 1, 2}, {5, 6, 2}};
+  static const int kTableBuild[2][3] = {{0, 1, 2}, {3, 4, 2}};
+  const int sw = sweep ? 1 : 0;
   const void *fn[3];
   for (int k = 0; k < 3; ++k)
-    fn[k] = (mode == 1 || mode == 2) ? rk4_f32_one_function(k, mode == 2)
-                                     : table_builds[mode == 3][k];
+    fn[k] = (mode == 1 || mode == 2) ? rk4_f32_one_function(kOneBuild[sw][k], mode == 2)
+                                     : table_builds[mode == 3][kTableBuild[sw][k]];
   if (rays_per_lane == 2) return fn[2];
   const int slot = (block >= 32 && block <= 256 && block % 32 == 0) ? block / 32 : 0;
-  int resident = slot ? g_resident_1[mode][slot].load(std::memory_order_relaxed) : 0;
+  int resident = slot ? g_resident_1[sw][mode][slot].load(std::memory_order_relaxed) : 0;
   if (resident == 0) {
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, fn[0], block, 0) !=
             cudaSuccess ||
@@ -190,7 +202,7 @@ const void *rk4_f32_function(int rays_per_lane, int block, int blocks_per_sm, in
       (void)cudaGetLastError();
       resident = blocks_per_sm;  // unknown: the uncapped build
     } else if (slot) {
-      g_resident_1[mode][slot].store(resident, std::memory_order_relaxed);
+      g_resident_1[sw][mode][slot].store(resident, std::memory_order_relaxed);
     }
   }
   return resident < blocks_per_sm ? fn[1] : fn[0];
@@ -206,7 +218,7 @@ cudaError_t launch_rk4_f32(const BatchArgs &a, int block, int blocks_per_sm, int
   const unsigned grid = static_cast<unsigned>(sms * blocks_per_sm);
   void *args[] = {const_cast<BatchArgs *>(&a)};
   const void *fn = rk4_f32_function(rays_per_lane, block, blocks_per_sm, a.n_scenarios,
-                                    a.all_same_grid, a.staging);
+                                    a.all_same_grid, a.staging, a.sweep_steps > 0);
   if (!fn) return cudaErrorInvalidValue;
   const size_t smem = a.staging == 1 ? rk4_f32_tile_smem(block)
                       : a.staging == 2 ? static_cast<size_t>(block) * 80 : 0;

@@ -20,6 +20,8 @@ static const void *one_build(int build) {
   switch (build) {
     case 0: return reinterpret_cast<const void *>(&rk4_f32_kernel_1<MODE>);
     case 1: return reinterpret_cast<const void *>(&rk4_f32_kernel_1r<MODE>);
+    case 5: return reinterpret_cast<const void *>(&rk4_f32_kernel_1s<MODE>);
+    case 6: return reinterpret_cast<const void *>(&rk4_f32_kernel_1rs<MODE>);
     default: return reinterpret_cast<const void *>(&rk4_f32_kernel_2<MODE>);
   }
 }

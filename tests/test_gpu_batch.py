@@ -502,6 +502,39 @@ def test_autotuner_candidates_cache_and_results(mr, tmp_path, monkeypatch):
         np.testing.assert_array_equal(x, y)
 
 
+def test_autotuner_long_stage_tries_sweeps(mr, monkeypatch):
+    # With a long stage the finalists are timed again on more rays over more
+    # steps, the ordered one-ray ones also in sweeps: the winner is a
+    # finalist or one of those sweep forms, probed on probe_rays rays.
+    from mantaray_gb300 import batch as B
+    from mantaray_gb300.workloads import seamount
+
+    w = seamount(n_rays=16384, steps=400)
+    tracer = B.BatchTracer([_fields(mr, w)])
+    ins = _dev(w.x0, w.y0, w.kx0, w.ky0)
+    monkeypatch.delenv("MANTARAY_TUNE_CACHE", raising=False)
+    monkeypatch.setattr(B, "_TUNE_CACHE", {})
+    cands = [B.make_config(64, 8, 1, 32, 0), B.make_config(128, 4, 1, 32, 1),
+             B.make_config(256, 2, 2, 32, 1)]
+    timed = []
+    real = B.BatchTracer.trace
+
+    def spy(self, x0, *a, **k):
+        cfg = a[8] if len(a) > 8 else k.get("config")  # (y0, kx0, ky0, dt, steps, t0, dec, sc, cfg)
+        timed.append((int(x0.numel()), cfg.as_dict()))
+        return real(self, x0, *a, **k)
+
+    monkeypatch.setattr(B.BatchTracer, "trace", spy)
+    cfg = tracer.autotune(*ins, w.dt, 100, candidates=cands, long_steps=400, long_rays=16384,
+                          finalists=2, sweeps=(64, 1000), probe_rays=4096)
+    allowed = [c.as_dict() for c in cands] + [dict(cands[1].as_dict(), sweep_steps=64)]
+    assert cfg.as_dict() in allowed
+    assert {n for n, _ in timed} == {4096, 16384}
+    long_cfgs = [c for n, c in timed if n == 16384]
+    assert dict(cands[1].as_dict(), sweep_steps=64) in long_cfgs  # 1000 > long_steps: not tried
+    assert all(c["sweep_steps"] in (0, 64) for c in long_cfgs)
+
+
 def test_decimation_tuner_budgets(mr):
     # The decimation tuner considers only the choices whose stored rows fit
     # the memory budget, times each, and takes the finest one within the
@@ -609,3 +642,103 @@ def test_staging_refused_where_it_does_not_apply(mr):
         two.trace(*ins, 1.0, 10, config=make_config(128, 4, 1, 32, 0, 3))
     with pytest.raises(MantarayError, match="one ray per lane"):
         BatchTracer([(b, c)]).trace(*ins, 1.0, 10, config=make_config(128, 4, 2, 32, 0, 1))
+
+
+def _bits(o):
+    return [o.end_state.cpu().numpy().view(np.uint64), o.n_steps.cpu().numpy(),
+            o.n_saved.cpu().numpy(), o.status.cpu().numpy(), o.saved.cpu().numpy().view(np.uint32)]
+
+
+@pytest.mark.parametrize("field", ["seamount", "shelf_slope"])
+def test_sweeps_give_identical_results(mr, field):
+    # The sweep form stops every ray after sweep_steps steps, stores its
+    # state, re-orders the running rays by where they are and takes them up
+    # again in the next launch.  A ray's arithmetic does not depend on the
+    # lane or the launch that runs it, so every output bit equals a single
+    # launch's: sweeps of 1 step, of a length that does not divide the
+    # horizon, of more steps than the horizon; through a captured graph
+    # replayed with fewer rays than its capacity.
+    from mantaray_gb300.batch import BatchTracer, make_config
+    from mantaray_gb300.workloads import seamount, shelf_slope
+
+    if field == "seamount":
+        w = seamount(n_rays=8192, steps=600)
+        b, c = _fields(mr, w)
+        rays, dt, steps = (w.x0, w.y0, w.kx0, w.ky0), w.dt, 600
+    else:
+        f, r = shelf_slope(n=1024, n_rays=8192, steps=3000, spacing=400.0)
+        b = mr.Bathymetry.grid(f[0], f[1], f[2])
+        c = mr.Current.grid(f[3], f[4], f[5], f[6])
+        rays, dt, steps = (r["x0"], r["y0"], r["kx0"], r["ky0"]), r["dt"], 3000
+    tracer = BatchTracer([(b, c)])
+    ins = _dev(*rays)
+    ref = _bits(tracer.trace(*ins, dt, steps, decimation=50, config=make_config(128, 4, 1, 32, 1)))
+    assert np.any(ref[3] != 0) and np.any(ref[3] == 0)  # rays end in different ways
+    for shape, sweep in (((128, 4, 1, 32, 1), 64), ((64, 8, 1, 32, 1), 37),
+                         ((256, 2, 1, 32, 1), steps + 5), ((128, 12, 1, 32, 1), 1 if steps <= 600 else 3)):
+        got = _bits(tracer.trace(*ins, dt, steps, decimation=50,
+                                 config=make_config(*shape, 0, sweep)))
+        for x, y in zip(got, ref):
+            np.testing.assert_array_equal(x, y)
+    g = tracer.graph(*ins, dt, steps, decimation=50, config=make_config(128, 6, 1, 32, 1, 0, 100))
+    g.launch()
+    for x, y in zip(_bits(g.out), ref):
+        np.testing.assert_array_equal(x, y)
+    # a replay with fewer rays: the first 3,000 rays' results, as a call of 3,000 rays
+    sub = _bits(tracer.trace(*[t[:3000] for t in ins], dt, steps, decimation=50,
+                             config=make_config(128, 4, 1, 32, 1)))
+    g.launch(3000)
+    got = _bits(g.out)
+    for x, y in zip(got[:4], sub[:4]):
+        np.testing.assert_array_equal(x[..., :3000], y)
+    np.testing.assert_array_equal(got[4][:, :, :3000], sub[4])
+    g.close()
+
+
+@pytest.mark.parametrize("same_grid", [True, False])
+def test_sweeps_across_scenarios(mr, same_grid):
+    # the scenario-table builds (mode 3: every current on its bathymetry's
+    # grid; mode 0: a current on its own grid) in sweeps: the same bits
+    from mantaray_gb300.batch import BatchTracer, make_config
+    from mantaray_gb300.workloads import multi_source
+
+    scen, rays = multi_source(n_sources=32, rays_per_source=128, n_scenarios=4, n=512,
+                              steps=1500)
+    pairs = []
+    for i, s in enumerate(scen):
+        cur = mr.Current.grid(*s[3:])
+        if not same_grid and i == 1:
+            xc = np.asarray(s[3], dtype=np.float64)[::2]
+            yc = np.asarray(s[4], dtype=np.float64)[::2]
+            cur = mr.Current.grid(xc, yc, np.asarray(s[5])[::2, ::2], np.asarray(s[6])[::2, ::2])
+        pairs.append((mr.Bathymetry.grid(*s[:3]), cur))
+    tracer = BatchTracer(pairs)
+    ins = _dev(rays["x0"], rays["y0"], rays["kx0"], rays["ky0"])
+    (sid,) = _dev(rays["scenario"])
+    ref = _bits(tracer.trace(*ins, rays["dt"], 1500, decimation=100, scenario=sid,
+                             config=make_config(128, 4, 1, 32, 1)))
+    for sweep in (50, 333):
+        got = _bits(tracer.trace(*ins, rays["dt"], 1500, decimation=100, scenario=sid,
+                                 config=make_config(128, 4, 1, 32, 1, 0, sweep)))
+        for x, y in zip(got, ref):
+            np.testing.assert_array_equal(x, y)
+
+
+def test_sweeps_refused_where_they_do_not_apply(mr):
+    from mantaray_gb300 import MantarayError
+    from mantaray_gb300.batch import BatchTracer, make_config
+
+    x = np.arange(40, dtype=np.float32) * 100.0
+    xd = x.astype(np.float64)
+    tracer = BatchTracer([(mr.Bathymetry.grid(x, x, np.full(1600, 500.0)),
+                           mr.Current.grid(xd, xd, np.zeros(1600), np.zeros(1600)))])
+    ins = _dev(np.full(64, 1000.0), np.full(64, 1500.0), np.full(64, 0.03), np.zeros(64))
+    for cfg in (make_config(128, 4, 1, 32, 0, 0, 16), make_config(128, 4, 2, 32, 1, 0, 16),
+                make_config(128, 4, 1, 32, 1, 2, 16)):
+        with pytest.raises(MantarayError, match="sweeps need order = 1"):
+            tracer.trace(*ins, 1.0, 10, config=cfg)
+    with pytest.raises(MantarayError, match="sweep_steps must be"):
+        tracer.trace(*ins, 1.0, 10, config=make_config(128, 4, 1, 32, 1, 0, -1))
+    # zero steps in sweeps: every ray ends at its start, complete
+    out = tracer.trace(*ins, 1.0, 0, config=make_config(128, 4, 1, 32, 1, 0, 16))
+    assert np.all(out.n_steps.cpu().numpy() == 0) and np.all(out.status.cpu().numpy() == 0)
