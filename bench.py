@@ -592,14 +592,27 @@ def last_finite_states(traj, nr):
     return traj[:, last, idx].cpu().numpy(), last.cpu().numpy()
 
 
-def batch_kernels_per_call(cfg, max_cells: int, n_scenarios: int, decimation: int) -> int:
+def batch_kernels_per_call(cfg, max_cells: int, n_scenarios: int, decimation: int,
+                           max_steps: int) -> int:
     """This project's kernels in one batched call: rk4_f32, the NaN fill of
     the decimated rows, and with ordering order_keys + 3 per 8-bit pass of the
-    sort key (direction 8 bits, Morton code 2 x cell bits, scenario bits)."""
+    sort key (direction 8 bits, Morton code 2 x cell bits, scenario bits); in
+    sweeps, each sweep after the first adds sweep_next, 3 per 8-bit pass of
+    the running rays' key (Morton code 2 x 2-cell-block bits, scenario bits)
+    and rk4_f32."""
     cbits = int(np.ceil(np.log2(max_cells))) if max_cells > 1 else 0
     sbits = int(np.ceil(np.log2(n_scenarios))) if n_scenarios > 1 else 0
     passes = (8 + 2 * min(cbits, 16) + sbits + 7) // 8
-    return 1 + (1 if decimation else 0) + ((1 + 3 * passes) if cfg.order else 0)
+    k = 1 + (1 if decimation else 0) + ((1 + 3 * passes) if cfg.order else 0)
+    if cfg.sweep_steps > 0:
+        blocks = (max_cells + 1) // 2
+        bbits = 0
+        while bbits < 15 and (1 << bbits) < blocks:
+            bbits += 1
+        sweep_passes = max(1, (2 * bbits + sbits + 7) // 8)
+        sweeps = max(1, -(-max_steps // cfg.sweep_steps))
+        k += (sweeps - 1) * (2 + 3 * sweep_passes)
+    return k
 
 
 def north_star_batched(args, dev, stream, flush) -> dict:
@@ -762,7 +775,7 @@ def north_star_batched(args, dev, stream, flush) -> dict:
             "rel_position_p99": float(np.nanpercentile(sens, 99)),
             "rel_position_max": float(np.nanmax(sens))},
         "roofline": roof, "clocks": clock,
-        "gpu_launches": args.ns_calls * batch_kernels_per_call(cfg, args.ns_grid - 1, 1, 0),
+        "gpu_launches": args.ns_calls * batch_kernels_per_call(cfg, args.ns_grid - 1, 1, 0, steps),
     }
 
 
@@ -931,7 +944,7 @@ def batched_arm(args, rank: int, world: int, local_rank: int):
             return n_all
 
     cmax = max(max(fs[2].shape) - 1 for fs in fields)
-    kernels_per_call = batch_kernels_per_call(cfg, cmax, len(handles), decimation)
+    kernels_per_call = batch_kernels_per_call(cfg, cmax, len(handles), decimation, steps)
     for i in range(args.warmup):
         one(i)
     torch.cuda.synchronize()

@@ -226,13 +226,14 @@ typedef struct mr_batch_config {
                           the call runs in sweeps of at most sweep_steps steps
                           per ray (ceil(max_steps / sweep_steps) launches);
                           between two sweeps the rays still running are sorted
-                          again by their current cell and direction, so that
+                          again by where they are (2 x 2-cell blocks), so that
                           the rays a GPU runs at once stay in one part of the
                           field and share its cell records in L2 (results per
                           ray are the same).  Needs order = 1, one ray per
-                          lane and MR_STAGING_NONE; the running rays' states
-                          take 68 bytes per ray of scratch, grown on demand
-                          by direct calls and owned by each graph. */
+                          lane and MR_STAGING_NONE; the running rays' states,
+                          list and sort keys take 76 bytes per ray of scratch,
+                          grown on demand by direct calls and owned by each
+                          graph. */
 } mr_batch_config;
 
 #define MR_STAGING_NONE 0

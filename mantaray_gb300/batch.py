@@ -137,7 +137,7 @@ class BatchTracer:
 
     def autotune(self, x0, y0, kx0, ky0, dt, probe_steps, t0=0.0, scenario=None,
                  candidates=None, repeats=2, cache_key=None, long_steps=None,
-                 long_rays=None, finalists=4, sweeps=(128, 256),
+                 long_rays=None, finalists=4, sweeps=(64, 96, 128),
                  probe_rays=None) -> N.BatchConfig:
         """Times every candidate launch shape on a probe run (the first
         `probe_rays` of the given rays, default all, for `probe_steps` steps,
@@ -146,10 +146,10 @@ class BatchTracer:
         first `long_rays` rays for `long_steps` steps, once each, and the
         fastest of that run wins: a short probe keeps the rays near their
         starts, where the fields they read may fit in L2, while a long trace
-        spreads them over the whole field.  There each ordered one-ray
-        finalist (and the fastest such candidate, if no finalist is one) is
-        also timed in sweeps of each length in `sweeps`, a form that only
-        pays once the rays have spread.  Results are cached in memory and in
+        spreads them over the whole field.  There the two fastest ordered
+        one-ray finalists (or the fastest such candidate, if no finalist is
+        one) are also timed in sweeps of each length in `sweeps`, a form that
+        only pays once the rays have spread.  Results are cached in memory and in
         $MANTARAY_TUNE_CACHE (a JSON file) when that is set."""
         torch = _torch()
         key = cache_key
@@ -209,7 +209,7 @@ class BatchTracer:
                 return c.order == 1 and c.rays_per_lane == 1 and c.staging == 0 and \
                     c.sweep_steps == 0
 
-            bases = [c for c in finals if sweepable(c)]
+            bases = [c for c in finals if sweepable(c)][:2]
             if not bases:
                 bases = [candidates[i] for _, i in ranked if sweepable(candidates[i])][:1]
             finals += [make_config(**dict(c.as_dict(), sweep_steps=sw))

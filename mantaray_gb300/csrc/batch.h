@@ -96,19 +96,26 @@ struct BatchArgs {
   const uint32_t *order;     // [n] ray taken at each queue slot, or null (slot = ray)
   // The sweep form (sweep_steps > 0): a launch advances each ray it takes by
   // at most sweep_steps steps; a ray still running then leaves its state in
-  // sweep[ray] and its index in next_list[*next_count] for the next launch.
-  // Every launch takes *n_dev rays in the order `order` (the first: the
-  // call's n rays; the later ones: the list, re-ordered).
+  // sweep[ray], and its index and sort key in next_list / next_keys at
+  // position *next_count (counted up) for the next launch.  Every launch
+  // takes *n_dev rays in the order `order` (the first: the call's n rays;
+  // the later ones: the list, sorted by key).  The key: the Morton code of
+  // the ray's 2 x 2-cell block on its scenario's bathymetry grid (sweep_cell_bits
+  // bits per axis), the scenario above it (bit sweep_key_shift up).
   int32_t sweep_steps;
   int32_t sweep_first;             // 1: the call's first launch (rays from x0, y0, kx0, ky0)
+  int32_t sweep_cell_bits;
+  int32_t sweep_key_shift;
   SweepRay *sweep;                 // [n_stride]
   uint32_t *next_list;             // [n_stride]
+  uint64_t *next_keys;             // [n_stride]
   unsigned long long *next_count;
   const int64_t *n_dev;
 };
 
 // Spatial ordering of the rays (order.cu): keys [2][n_max] and values
-// [2][n_max] ping-pong buffers, per-tile digit counts [256][tiles].
+// [2][n_max] ping-pong buffers, per-tile digit counts [256][tiles], digit
+// totals [256].
 constexpr int kOrderTile = 4096;
 struct OrderArgs {
   const ScenarioDev *scen;
@@ -120,13 +127,13 @@ struct OrderArgs {
   uint64_t *keys[2];
   uint32_t *vals[2];
   uint32_t *counts;
+  uint32_t *totals;          // [256] rays per digit of the current pass
   int tiles;                 // ceil(capacity / kOrderTile)
   int scen_shift;            // bit position of the scenario in the key
-  // the sweep form: order the *n_dev rays list[0 .. *n_dev) by the cell and
-  // direction of their current state in sweep[] (null: the n rays by their
-  // initial states)
-  const uint32_t *list;
-  const SweepRay *sweep;
+  // keys and values sorted by the first pass when order_keys does not run
+  // (the sweep form: the keys the batched kernel wrote); null: keys[0], vals[0]
+  const uint64_t *in_keys;
+  const uint32_t *in_vals;
 };
 
 }  // namespace mr

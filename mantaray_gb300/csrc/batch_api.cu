@@ -154,15 +154,17 @@ cudaError_t sweep_reserve(mr_order_buffers *o, size_t n) {
   o->sweep_mem = nullptr;
   o->sweep_cap = 0;
   auto up = [](size_t v) { return (v + 255) & ~static_cast<size_t>(255); };
-  const size_t states = up(n * sizeof(mr::SweepRay));
+  const size_t states = up(n * sizeof(mr::SweepRay)), keys = up(n * sizeof(uint64_t));
   char *p = nullptr;
-  cudaError_t e = cudaMalloc(reinterpret_cast<void **>(&p), 256 + states + up(n * sizeof(uint32_t)));
+  cudaError_t e = cudaMalloc(reinterpret_cast<void **>(&p),
+                             256 + states + keys + up(n * sizeof(uint32_t)));
   if (e != cudaSuccess) return e;
   o->sweep_mem = p;
   o->sweep_cap = n;
   o->count = reinterpret_cast<unsigned long long *>(p);
   o->sweep = reinterpret_cast<mr::SweepRay *>(p + 256);
-  o->list = reinterpret_cast<uint32_t *>(p + 256 + states);
+  o->list_keys = reinterpret_cast<uint64_t *>(p + 256 + states);
+  o->list = reinterpret_cast<uint32_t *>(p + 256 + states + keys);
   return cudaSuccess;
 }
 
@@ -176,7 +178,8 @@ cudaError_t order_reserve(mr_order_buffers *o, size_t n) {
   const size_t keys = up(n * sizeof(uint64_t)), vals = up(n * sizeof(uint32_t));
   const size_t counts = up(256ull * tiles * sizeof(uint32_t));
   char *p = nullptr;
-  cudaError_t e = cudaMalloc(reinterpret_cast<void **>(&p), 256 + 2 * keys + 2 * vals + counts);
+  cudaError_t e = cudaMalloc(reinterpret_cast<void **>(&p),
+                             256 + 2 * keys + 2 * vals + counts + 256 * sizeof(uint32_t));
   if (e != cudaSuccess) return e;
   o->mem = p;
   o->cap = n;
@@ -187,6 +190,7 @@ cudaError_t order_reserve(mr_order_buffers *o, size_t n) {
   o->vals[0] = reinterpret_cast<uint32_t *>(p + 256 + 2 * keys);
   o->vals[1] = reinterpret_cast<uint32_t *>(p + 256 + 2 * keys + vals);
   o->counts = reinterpret_cast<uint32_t *>(p + 256 + 2 * keys + 2 * vals);
+  o->totals = reinterpret_cast<uint32_t *>(p + 256 + 2 * keys + 2 * vals + counts);
   return cudaSuccess;
 }
 
@@ -201,6 +205,7 @@ mr::OrderArgs order_args(const mr_batch *b, const mr::BatchArgs &a, const mr_ord
   r.keys[0] = o.keys[0]; r.keys[1] = o.keys[1];
   r.vals[0] = o.vals[0]; r.vals[1] = o.vals[1];
   r.counts = o.counts;
+  r.totals = o.totals;
   r.tiles = o.tiles;
   r.scen_shift = b->order_scen_shift;
   return r;
@@ -340,21 +345,26 @@ cudaError_t enqueue(const mr_batch *b, mr::BatchArgs *a, const mr_batch_config *
   if (e != cudaSuccess) return e;
   a->sweep_steps = cfg->sweep_steps;
   a->sweep_first = 1;
+  a->sweep_cell_bits = b->sweep_cell_bits;
+  a->sweep_key_shift = b->sweep_key_shift;
   a->sweep = ord->sweep;
   a->next_list = ord->list;
+  a->next_keys = ord->list_keys;
   a->next_count = ord->count;
   a->n_dev = ord->n_dev;
   e = mr::launch_rk4_f32(*a, cfg->block, cfg->blocks_per_sm, cfg->rays_per_lane, s);
   if (e != cudaSuccess) return e;
+  // later launches: the list sorted by the keys the kernel wrote
   mr::BatchArgs later = *a;
   later.sweep_first = 0;
+  later.order = ord->vals[b->sweep_passes & 1];
   mr::OrderArgs ol = o;
-  ol.list = ord->list;
-  ol.sweep = ord->sweep;
+  ol.in_keys = ord->list_keys;
+  ol.in_vals = ord->list;
   const int64_t sweeps = (a->max_steps + cfg->sweep_steps - 1) / cfg->sweep_steps;
   for (int64_t k = 1; k < sweeps; ++k) {
     e = mr::launch_sweep_next(ord->n_dev, ord->count, a->queue, s);
-    if (e == cudaSuccess) e = mr::launch_order(ol, a->n_stride, b->order_passes, s);
+    if (e == cudaSuccess) e = mr::launch_order(ol, a->n_stride, b->sweep_passes, s);
     if (e == cudaSuccess)
       e = mr::launch_rk4_f32(later, cfg->block, cfg->blocks_per_sm, cfg->rays_per_lane, s);
     if (e != cudaSuccess) return e;
@@ -441,6 +451,13 @@ int mr_batch_create(size_t n_scenarios, const mr_bathymetry *const *bathy,
     while ((1 << sbits) < b->n_scenarios) ++sbits;
     b->order_scen_shift = 8 + 2 * cbits;
     b->order_passes = (b->order_scen_shift + sbits + 7) / 8;
+    // the sweep form's key: the Morton code of the 2 x 2-cell block (no
+    // direction), the scenario above it
+    int bbits = 0;
+    while (bbits < 15 && (1 << bbits) < (cmax + 1) / 2) ++bbits;
+    b->sweep_cell_bits = bbits;
+    b->sweep_key_shift = 2 * bbits;
+    b->sweep_passes = std::max(1, (2 * bbits + sbits + 7) / 8);
   }
   if (rc == MR_OK && e == cudaSuccess && n_scenarios == 1 && b->host_scen[0].same_grid) {
     const mr::ScenarioDev &sc = b->host_scen[0];
@@ -551,9 +568,8 @@ int mr_batch_graph_create(mr_batch *b, size_t n_max, const uint8_t *ray_scenario
       e = cudaGraphKernelNodeGetParams(nodes[i], &p);
       if (e != cudaSuccess) break;
       // the ordering of the call's rays (a sweep form's later orderings
-      // take their rays from the list and n from the device)
-      if (p.func == mr::order_keys_function() &&
-          static_cast<const mr::OrderArgs *>(p.kernelParams[0])->list == nullptr) {
+      // sort the keys its kernel wrote: no order_keys)
+      if (p.func == mr::order_keys_function()) {
         gr->order_node = nodes[i];
         gr->order_params = p;
       } else if (p.func == k2 && !gr->kernel_node) {

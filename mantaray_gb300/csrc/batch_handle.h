@@ -9,9 +9,9 @@
 
 // Device scratch of the spatial ordering (order.cu) for up to `cap` rays:
 // one allocation holding n_dev, keys [2][cap], vals [2][cap], counts
-// [256][tiles]; and for the sweep form, for up to `sweep_cap` rays, another
-// holding the list counter, the running rays' states [sweep_cap] and the
-// list [sweep_cap].
+// [256][tiles], totals [256]; and for the sweep form, for up to `sweep_cap` rays, another
+// holding the list counter, the running rays' states [sweep_cap], the list
+// [sweep_cap] and its sort keys [sweep_cap].
 struct mr_order_buffers {
   void *mem = nullptr;
   size_t cap = 0;
@@ -20,11 +20,13 @@ struct mr_order_buffers {
   uint64_t *keys[2] = {nullptr, nullptr};
   uint32_t *vals[2] = {nullptr, nullptr};
   uint32_t *counts = nullptr;
+  uint32_t *totals = nullptr;
   void *sweep_mem = nullptr;
   size_t sweep_cap = 0;
   unsigned long long *count = nullptr;
   mr::SweepRay *sweep = nullptr;
   uint32_t *list = nullptr;
+  uint64_t *list_keys = nullptr;
 };
 
 struct mr_batch {
@@ -37,6 +39,9 @@ struct mr_batch {
   mr_order_buffers ord;              // ordering scratch of direct calls, grown on demand
   int order_scen_shift = 8;          // key layout of the ordering (order.cu)
   int order_passes = 1;
+  int sweep_cell_bits = 0;           // key layout of the sweep form's orderings (k2.cuh)
+  int sweep_key_shift = 0;
+  int sweep_passes = 1;
   // tensor maps of the cell records for the tile build (one scenario with its
   // current on the bathymetry's grid), made at creation
   CUtensorMap tmap_bathy{};

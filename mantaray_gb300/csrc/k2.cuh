@@ -620,6 +620,39 @@ __device__ __forceinline__ void resume(const BatchArgs &a, RayLane &L, int64_t r
   L.limit = static_cast<int32_t>(lim < a.max_steps ? lim : a.max_steps);
 }
 
+// Bits 0-15 of v spread to the even bits of the result.
+__device__ __forceinline__ uint32_t spread_even16(uint32_t v) {
+  v &= 0xffffu;
+  v = (v | (v << 8)) & 0x00ff00ffu;
+  v = (v | (v << 4)) & 0x0f0f0f0fu;
+  v = (v | (v << 2)) & 0x33333333u;
+  v = (v | (v << 1)) & 0x55555555u;
+  return v;
+}
+
+// The 2 x 2-cell block of v on an axis (first value v0, 1 / spacing inv),
+// clamped to 0..lim; NaN gives 0.  Only an ordering key: no exactness needed.
+__device__ __forceinline__ uint32_t sweep_block(double v, double v0, double inv, uint32_t lim) {
+  const double c = floor((v - v0) * inv);
+  if (!(c > 0.0)) return 0u;
+  const double b = c * 0.5;
+  return b >= static_cast<double>(lim) ? lim : static_cast<uint32_t>(b);
+}
+
+// The sweep form's sort key of a running ray: the Morton code of its 2 x 2
+// block of bathymetry cells, its scenario above it (BatchArgs::sweep_*).
+__device__ __forceinline__ uint64_t sweep_key(const BatchArgs &a, const ScenarioDev &s,
+                                              const RayLane &L) {
+  const PackedGrid &g = s.bathy;
+  const uint32_t lim = (1u << a.sweep_cell_bits) - 1u;
+  const uint32_t bx = sweep_block(L.ox + (static_cast<double>(L.px) - static_cast<double>(L.cpx)),
+                                  g.x0, g.inv_sp_xd, lim);
+  const uint32_t by = sweep_block(L.oy + (static_cast<double>(L.py) - static_cast<double>(L.cpy)),
+                                  g.y0, g.inv_sp_yd, lim);
+  return (static_cast<uint64_t>(L.scen) << a.sweep_key_shift) |
+         static_cast<uint64_t>(spread_even16(bx) | (spread_even16(by) << 1));
+}
+
 __device__ __forceinline__ void store_sweep(const BatchArgs &a, const RayLane &L) {
   float4 *p = reinterpret_cast<float4 *>(a.sweep + L.ray);
   *reinterpret_cast<double2 *>(p) = make_double2(L.ox, L.oy);
@@ -735,8 +768,8 @@ __device__ __forceinline__ void k2_body(const BatchArgs &a) {
   int iter = 0;
   while (true) {
     if (SWEEP) {
-      // rays at the end of this launch's sweep: state out, listed for the
-      // next launch (one atomic per warp)
+      // rays at the end of this launch's sweep: state out, listed with
+      // their sort key for the next launch (one atomic per warp)
       const bool out = L[0].ray >= 0 && L[0].step >= L[0].limit && L[0].step < max_steps;
       const unsigned leaving = __ballot_sync(kFull, out);
       if (leaving) {
@@ -747,7 +780,9 @@ __device__ __forceinline__ void k2_body(const BatchArgs &a) {
         base = __shfl_sync(kFull, base, leader);
         if (out) {
           store_sweep(a, L[0]);
-          a.next_list[base + __popc(leaving & lt_mask)] = static_cast<uint32_t>(L[0].ray);
+          const unsigned long long pos = base + __popc(leaving & lt_mask);
+          a.next_list[pos] = static_cast<uint32_t>(L[0].ray);
+          a.next_keys[pos] = sweep_key(a, scenario<MODE>(a, L[0].scen), L[0]);
           L[0].ray = -1;
         }
       }

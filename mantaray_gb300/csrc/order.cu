@@ -10,13 +10,18 @@
 // directions and stay close for many steps, so their cell reads are shared.
 // Each ray's result is unchanged: its arithmetic does not depend on its lane,
 // its neighbours or when it is taken; only the order of the queue changes.
+// The sweep form sorts the rays still running between two launches the same
+// way, by keys the batched kernel wrote when it stopped them (the Morton code
+// of their current 2 x 2-cell block): order_keys does not run, the first
+// pass reads those keys, and sweep_next moves their count into n_dev.
 //
 // All kernels run over grids sized for a capacity n_max, so one captured
 // graph replays them for any n <= n_max: order_keys takes n as its argument
 // and stores it in device memory, where the later kernels read it.
 //   order_keys     one thread per ray: key and identity value
 //   order_hist     one block per tile of kTile rays: digit counts, [digit][tile]
-//   order_scan     one block: exclusive scan of the counts in [digit][tile] order
+//   order_scan     one block per digit: exclusive scan of its counts over the
+//                  tiles, and its total
 //   order_scatter  one block per tile: stable scatter of (key, value) by digit
 // Stability within a tile: rounds of 256 consecutive rays; inside a round a
 // ray's rank among equal digits is its rank within its warp
@@ -35,7 +40,7 @@ namespace {
 
 constexpr int kOrderThreads = 256;
 constexpr int kOrderWarps = kOrderThreads / 32;
-constexpr int kScanThreads = 1024;
+constexpr int kScanThreads = 256;
 
 // Bits 0-15 of v spread to the even bits of the result.
 __device__ __forceinline__ uint32_t spread16(uint32_t v) {
@@ -69,41 +74,16 @@ __device__ __forceinline__ uint64_t order_key(const OrderArgs &o, int s, double 
          static_cast<uint64_t>(tb);
 }
 
-// Grid-stride over the rays (a fixed grid: a sweep's list is usually far
-// shorter than the capacity).  Without a list: the n rays by their initial
-// states, n stored for the later kernels.  With one: the *n_dev listed rays
-// by their current states (position origin + offset, as the batched kernel
-// stores it; wavenumber without its compensation: a key needs no more).
+// The n rays by their initial states, n stored for the later kernels;
+// grid-stride over a fixed grid.
 __global__ void order_keys(OrderArgs o) {
-  int64_t n;
-  if (o.list) {
-    n = *o.n_dev;
-  } else {
-    n = o.n;
-    if (blockIdx.x == 0 && threadIdx.x == 0) *o.n_dev = o.n;
-  }
-  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
-       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    uint32_t ray;
-    double x, y;
-    float kx, ky;
-    if (o.list) {
-      ray = o.list[i];
-      const SweepRay &S = o.sweep[ray];
-      x = S.ox + (static_cast<double>(S.px) - static_cast<double>(S.cpx));
-      y = S.oy + (static_cast<double>(S.py) - static_cast<double>(S.cpy));
-      kx = S.kx;
-      ky = S.ky;
-    } else {
-      ray = static_cast<uint32_t>(i);
-      x = o.x0[i];
-      y = o.y0[i];
-      kx = static_cast<float>(o.kx0[i]);
-      ky = static_cast<float>(o.ky0[i]);
-    }
-    const int s = o.ray_scenario ? static_cast<int>(o.ray_scenario[ray]) : 0;
-    o.keys[0][i] = order_key(o, s, x, y, kx, ky);
-    o.vals[0][i] = ray;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *o.n_dev = o.n;
+  for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < o.n;
+       r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int s = o.ray_scenario ? static_cast<int>(o.ray_scenario[r]) : 0;
+    o.keys[0][r] = order_key(o, s, o.x0[r], o.y0[r], static_cast<float>(o.kx0[r]),
+                             static_cast<float>(o.ky0[r]));
+    o.vals[0][r] = static_cast<uint32_t>(r);
   }
 }
 
@@ -114,7 +94,7 @@ __global__ void __launch_bounds__(kOrderThreads) order_hist(OrderArgs o, int pas
   __syncthreads();
   const int64_t n = *o.n_dev;
   const int shift = 8 * pass;
-  const uint64_t *keys = o.keys[pass & 1];
+  const uint64_t *keys = (pass == 0 && o.in_keys) ? o.in_keys : o.keys[pass & 1];
   const int64_t start = static_cast<int64_t>(blockIdx.x) * kOrderTile;
   for (int i = t; i < kOrderTile; i += kOrderThreads) {
     const int64_t e = start + i;
@@ -125,30 +105,23 @@ __global__ void __launch_bounds__(kOrderThreads) order_hist(OrderArgs o, int pas
   o.counts[static_cast<int64_t>(t) * o.tiles + blockIdx.x] = h[t];
 }
 
-// Exclusive scan in place of the digit counts [256][tiles], digit-major, over
-// the tiles that hold rays (the first ceil(n / kOrderTile)), by one block in
-// chunks of 4 * kScanThreads.
+// Exclusive scan in place of one digit's counts over the tiles that hold
+// rays (the first ceil(n / kOrderTile) of its row of counts [256][tiles]),
+// one block per digit, and the digit's total to totals[digit].  The scatter
+// adds the digits' own offsets (a scan of the 256 totals).
 __global__ void __launch_bounds__(kScanThreads) order_scan(OrderArgs o) {
   __shared__ unsigned warp_sum[kScanThreads / 32];
   __shared__ unsigned carry_s;
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-  // only the tiles that hold rays: the counts of the others are never read
   const int64_t n = *o.n_dev;
   const int used = static_cast<int>((n + kOrderTile - 1) / kOrderTile);
-  const int64_t total = 256ll * used;
-  auto at = [&](int64_t i) -> uint32_t & {  // i < 256 * used < 2^32
-    const uint32_t u = static_cast<uint32_t>(i), d = u / static_cast<uint32_t>(used);
-    return o.counts[static_cast<int64_t>(d) * o.tiles + (u - d * static_cast<uint32_t>(used))];
-  };
+  uint32_t *row = o.counts + static_cast<int64_t>(blockIdx.x) * o.tiles;
   if (t == 0) carry_s = 0u;
   __syncthreads();
-  for (int64_t base = 0; base < total; base += 4ll * kScanThreads) {
-    const int64_t i0 = base + 4ll * t;
-    unsigned v[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) v[k] = (i0 + k < total) ? at(i0 + k) : 0u;
-    const unsigned local = v[0] + v[1] + v[2] + v[3];
-    unsigned incl = local;  // inclusive scan across the warp
+  for (int i0 = 0; i0 < used; i0 += kScanThreads) {
+    const int i = i0 + t;
+    const unsigned v = i < used ? row[i] : 0u;
+    unsigned incl = v;  // inclusive scan across the warp
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
       const unsigned up = __shfl_up_sync(0xffffffffu, incl, d);
@@ -157,26 +130,23 @@ __global__ void __launch_bounds__(kScanThreads) order_scan(OrderArgs o) {
     if (lane == 31) warp_sum[w] = incl;
     __syncthreads();
     if (w == 0) {
-      unsigned ws = warp_sum[lane];
+      const unsigned ws = lane < kScanThreads / 32 ? warp_sum[lane] : 0u;
       unsigned wi = ws;
 #pragma unroll
       for (int d = 1; d < 32; d <<= 1) {
         const unsigned up = __shfl_up_sync(0xffffffffu, wi, d);
         if (lane >= d) wi += up;
       }
-      warp_sum[lane] = wi - ws;  // exclusive prefix of the warp sums
+      if (lane < kScanThreads / 32) warp_sum[lane] = wi - ws;  // exclusive prefix of the warp sums
     }
     __syncthreads();
-    unsigned run = carry_s + warp_sum[w] + (incl - local);
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      if (i0 + k < total) at(i0 + k) = run;
-      run += v[k];
-    }
+    const unsigned before = carry_s + warp_sum[w] + (incl - v);
+    if (i < used) row[i] = before;
     __syncthreads();
-    if (t == kScanThreads - 1) carry_s = run;
+    if (t == kScanThreads - 1) carry_s = before + v;
     __syncthreads();
   }
+  if (t == 0) o.totals[blockIdx.x] = carry_s;
 }
 
 __global__ void __launch_bounds__(kOrderThreads) order_scatter(OrderArgs o, int pass) {
@@ -186,13 +156,31 @@ __global__ void __launch_bounds__(kOrderThreads) order_scatter(OrderArgs o, int 
   const unsigned lt = (1u << lane) - 1u;
   const int64_t n = *o.n_dev;
   const int shift = 8 * pass;
-  const uint64_t *kin = o.keys[pass & 1];
-  const uint32_t *vin = o.vals[pass & 1];
+  const uint64_t *kin = (pass == 0 && o.in_keys) ? o.in_keys : o.keys[pass & 1];
+  const uint32_t *vin = (pass == 0 && o.in_keys) ? o.in_vals : o.vals[pass & 1];
   uint64_t *kout = o.keys[(pass & 1) ^ 1];
   uint32_t *vout = o.vals[(pass & 1) ^ 1];
   const int64_t start = static_cast<int64_t>(blockIdx.x) * kOrderTile;
-  base[t] = o.counts[static_cast<int64_t>(t) * o.tiles + blockIdx.x];
-  run[t] = 0u;
+  if (start >= n) return;  // uniform in the block
+  {
+    // where digit t starts: the totals of the smaller digits (an exclusive
+    // scan of the 256 totals, the same in every block) plus this tile's
+    // offset within the digit
+    const unsigned v = o.totals[t];
+    unsigned incl = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const unsigned up = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= d) incl += up;
+    }
+    if (lane == 31) wcnt[0][w] = incl;
+    __syncthreads();
+    unsigned before = incl - v;
+    for (int q = 0; q < w; ++q) before += wcnt[0][q];
+    base[t] = before + o.counts[static_cast<int64_t>(t) * o.tiles + blockIdx.x];
+    run[t] = 0u;
+    __syncthreads();
+  }
   for (int j = 0; j < kOrderTile / kOrderThreads; ++j) {
     if (start + static_cast<int64_t>(j) * kOrderThreads >= n) break;  // uniform in the block
 #pragma unroll
@@ -250,16 +238,18 @@ int order_tiles(int64_t n_max) {
 
 cudaError_t launch_order(const OrderArgs &o, int64_t n_max, int passes, cudaStream_t stream) {
   if (n_max <= 0) return cudaSuccess;
-  int dev = 0, sms = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (e != cudaSuccess) return e;
-  const int64_t blocks = (n_max + kOrderThreads - 1) / kOrderThreads;
-  const unsigned kgrid = static_cast<unsigned>(blocks < 8ll * sms ? blocks : 8ll * sms);
-  order_keys<<<kgrid, kOrderThreads, 0, stream>>>(o);
+  if (!o.in_keys) {
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    const int64_t blocks = (n_max + kOrderThreads - 1) / kOrderThreads;
+    const unsigned kgrid = static_cast<unsigned>(blocks < 8ll * sms ? blocks : 8ll * sms);
+    order_keys<<<kgrid, kOrderThreads, 0, stream>>>(o);
+  }
   for (int p = 0; p < passes; ++p) {
     order_hist<<<o.tiles, kOrderThreads, 0, stream>>>(o, p);
-    order_scan<<<1, kScanThreads, 0, stream>>>(o);
+    order_scan<<<256, kScanThreads, 0, stream>>>(o);
     order_scatter<<<o.tiles, kOrderThreads, 0, stream>>>(o, p);
   }
   return cudaGetLastError();
