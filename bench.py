@@ -55,11 +55,12 @@ ALG_FP64_FLOP_PER_RAY_STEP = 270.0
 ALG_FP32_FLOP_PER_RAY_STEP = 710.0
 # FP64 floating-point operations one ray-step executes (DADD/DMUL = 1,
 # DFMA = 2), per right-hand-side arithmetic, counted by ncu on the plain
-# kernel over the seamount workload (65,536 rays x 100 steps)
-# (sm__sass_thread_inst_executed_op_d{add,mul,fma}_pred_on).
-FP64_FLOP_PER_RAY_STEP = {"libm": 1401.4, "identity": 219.3}
-# FP64-pipe instructions per ray-step (sm__inst_executed_pipe_fp64 x 32, same captures)
-FP64_PIPE_INST_PER_RAY_STEP = {"libm": 945.2, "identity": 195.4}
+# kernel over the seamount workload's whole 4,000-step horizon (20,480 of its
+# rays, 79.3 M ray-steps; sm__sass_thread_inst_executed_op_d{add,mul,fma}_pred_on).
+FP64_FLOP_PER_RAY_STEP = {"libm": 1399.1, "identity": 221.9}
+# FP64-pipe instructions per ray-step (sm__inst_executed_pipe_fp64 x 32: warp
+# instructions in lane slots, so lanes idle in a divergent warp count; same captures)
+FP64_PIPE_INST_PER_RAY_STEP = {"libm": 974.4, "identity": 223.4}
 # DRAM bytes (read + written) per ray-step of the plain kernel on the seamount
 # workload: ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch
 # over its 65,536 rays x 1,000 steps (55.5 MB read, 2,573.7 MB written: the
@@ -69,14 +70,28 @@ K1_DRAM_NOTE = ("ncu DRAM bytes of a 65,536-ray x 1,000-step launch of the same 
                 "(55.5 MB read, 2,573.7 MB written) scaled by ray-steps; rows still in L2 at the "
                 "end of that launch (at most 129 MB) are not counted")
 # The same for the batched kernel on the shelf-slope field: one graph-replayed
-# call of 262,144 rays traced to their ends on the field's generator at
-# 4,096^2 (records 1.3 GB, 10x L2; 3.10 G ray-steps; 161.04 GB read, 0.09 GB
-# written).  Its rays spread over the field as the benchmark's do on 8,192^2,
-# and a ray entering a new cell reads that cell's records from DRAM in both,
-# so the bytes scale with ray-steps.
-K2_SHELF_DRAM_BYTES_PER_RAY_STEP = (161042433536 + 93049344) / 3103336576
-K2_SHELF_DRAM_NOTE = ("ncu DRAM bytes of one call of the same generator at 4,096^2 (262,144 rays "
-                      "to their ends, 51.9 B per ray-step), scaled by this call's ray-steps")
+# call on the field's generator at 4,096^2 (records 1.3 GB, 10x L2) with the
+# 8,192^2 case's ray density, 5,466,581 rays traced to their ends (49.64 G
+# ray-steps), launch 128 x 12, ordered: the sum over the call's K2 launches,
+# by sweep length (0: one launch; in sweeps the bytes include the running
+# rays' states written and read between sweeps).  Its rays spread over the
+# field as the 8,192^2 case's do, so the bytes scale with ray-steps.
+K2_SHELF_RAY_STEPS = 49640953115
+K2_SHELF_DRAM_BYTES = {0: (1690693872640, 1447764224), 128: (103553328384, 28901769472),
+                       256: (61612061696, 15217717760)}
+
+
+def k2_shelf_dram(sweep_steps: int):
+    """DRAM bytes per ray-step of the batched kernel on the shelf-slope field
+    for a sweep length (the nearest captured one), and its note."""
+    s = 0
+    if sweep_steps > 0:
+        s = min((k for k in K2_SHELF_DRAM_BYTES if k > 0), key=lambda k: abs(k - sweep_steps))
+    rd, wr = K2_SHELF_DRAM_BYTES[s]
+    return (rd + wr) / K2_SHELF_RAY_STEPS, (
+        f"ncu DRAM bytes of one call of the same generator at 4,096^2 and the same ray density "
+        f"({'one launch' if s == 0 else f'sweeps of {s} steps'}; {(rd + wr) / K2_SHELF_RAY_STEPS:.2f} B "
+        f"per ray-step), scaled by this call's ray-steps")
 
 
 def parse():
@@ -727,20 +742,23 @@ def north_star_batched(args, dev, stream, flush) -> dict:
             "flop_per_ray_step": ALG_FP32_FLOP_PER_RAY_STEP,
             "executed_flop_per_ray_step": FP32_FLOP_PER_RAY_STEP,
             "executed_frac": value * FP32_FLOP_PER_RAY_STEP / 1e12 / fp32_peak.value}
-    if K2_SHELF_DRAM_BYTES_PER_RAY_STEP is not None:
-        roof["traffic"] = K2_SHELF_DRAM_BYTES_PER_RAY_STEP * done / args.ns_calls
-        roof["traffic_note"] = K2_SHELF_DRAM_NOTE
-        try:
-            hbm_peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
-            src = "MEASURED_PEAKS.json hbm_gbs"
-        except (OSError, ValueError, KeyError):
-            hbm_peak, src = 6800.0, "fallback"
-        gbs = K2_SHELF_DRAM_BYTES_PER_RAY_STEP * value / 1e9
-        roof["hbm"] = {"achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
-                       "peak_source": src,
-                       "note": "the DRAM reads of cell records on cell changes (L2 hit rate 27% "
-                               "in the capture): bound by their latency, neither this bandwidth "
-                               "nor the FP32 pipe is saturated"}
+    per_step, note = k2_shelf_dram(cfg.sweep_steps)
+    roof["traffic"] = per_step * done / args.ns_calls
+    roof["traffic_note"] = note
+    try:
+        hbm_peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
+        src = "MEASURED_PEAKS.json hbm_gbs"
+    except (OSError, ValueError, KeyError):
+        hbm_peak, src = 6800.0, "fallback"
+    gbs = per_step * value / 1e9
+    roof["hbm"] = {"achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
+                   "peak_source": src,
+                   "note": ("in sweeps the cell records mostly come from L2 (80% hits in the "
+                            "capture): issue-bound, like the fields that fit in L2"
+                            if cfg.sweep_steps else
+                            "the DRAM reads of cell records on cell changes (40% L2 hits in "
+                            "the capture): bound by their latency, neither this bandwidth "
+                            "nor the FP32 pipe is saturated")}
     roof["traffic_floor"] = float(np.mean(timed_counts)) * (4 * 8 + 5 * 8 + 4 + 4 + 1)
     status = np.bincount(stat_b, minlength=4)
     return {
