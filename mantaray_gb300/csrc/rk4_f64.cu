@@ -20,6 +20,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #include "kernels.h"
 #include "ray_exact.cuh"
 
@@ -131,6 +133,29 @@ __global__ void __launch_bounds__(kK1Block) rk4_f64_kernel(BathyDev b, CurrentDe
 
 }  // namespace
 
+// Resident blocks per SM of the cached build, by stop rule, arithmetic and
+// block size (8, 16, 32, 64), queried once; 0 when the query fails (no
+// cache).
+static int cached_resident(int stop_rule, int identity_math, int block) {
+  static std::atomic<int> known[2][2][4];
+  const int slot = block >= 64 ? 3 : block >= 32 ? 2 : block >= 16 ? 1 : 0;
+  std::atomic<int> &k = known[stop_rule == 1][identity_math != 0][slot];
+  int r = k.load(std::memory_order_relaxed);
+  if (r) return r < 0 ? 0 : r;
+  const void *fn =
+      stop_rule == 1
+          ? (identity_math ? reinterpret_cast<const void *>(&rk4_f64_kernel<1, RhsIdentity, LookupCache>)
+                           : reinterpret_cast<const void *>(&rk4_f64_kernel<1, RhsLibm, LookupCache>))
+          : (identity_math ? reinterpret_cast<const void *>(&rk4_f64_kernel<0, RhsIdentity, LookupCache>)
+                           : reinterpret_cast<const void *>(&rk4_f64_kernel<0, RhsLibm, LookupCache>));
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, fn, block, 0) != cudaSuccess || r < 1) {
+    (void)cudaGetLastError();
+    r = -1;
+  }
+  k.store(r, std::memory_order_relaxed);
+  return r < 0 ? 0 : r;
+}
+
 template <typename Rhs, typename Cache>
 static void launch_k1(int stop_rule, unsigned grid, int block, const BathyDev &b,
                       const CurrentDev &c, const TraceArgs &a, cudaStream_t stream) {
@@ -153,11 +178,14 @@ cudaError_t launch_rk4_f64(const BathyDev &b, const CurrentDev &c, const TraceAr
   int block = kK1Block;
   while (block > 8 && (a.n + block - 1) / block < static_cast<uint64_t>(sms)) block /= 2;
   const unsigned grid = static_cast<unsigned>((a.n + block - 1) / block);
-  // With at most two blocks per SM the rays' dependent chains, not the FP64
-  // pipe, set the time: the lookup cache shortens them (1,024-16,384 rays:
-  // 6-18% faster).  With more blocks the cache's registers (~150 a thread
-  // against ~100) cost resident blocks (65,536 rays: 26% slower).
-  const bool cache = grid <= 2u * static_cast<unsigned>(sms);
+  // The lookup cache shortens the rays' dependent chains (1,024-16,384 rays:
+  // 6-18% faster; the 65,536-ray seamount, identity arithmetic: 2.09 ->
+  // 2.15 G ray-steps/s, bit-identical) but takes registers (identity 128 a
+  // thread, libm 148, against 96 and 116).  It pays while every block of the
+  // call is resident at once: a second wave of blocks costs more than the
+  // cache saves (65,536 rays, libm: 26% slower).
+  const bool cache = grid <= static_cast<unsigned>(cached_resident(stop_rule, identity_math, block)) *
+                                 static_cast<unsigned>(sms);
   if (identity_math) {
     if (cache)
       launch_k1<RhsIdentity, LookupCache>(stop_rule, grid, block, b, c, a, stream);

@@ -366,13 +366,27 @@ def test_seamount_full_size_properties(mr, oracle):
     oc = oracle.Current.grid(w.cx, w.cy, w.u, w.v)
     o = oracle.trace(ob, oc, w.x0[idx], w.y0[idx], w.kx0[idx], w.ky0[idx], w.t0, w.t_end, w.dt)
     H.assert_parity(np.ascontiguousarray(sub), rows1[idx], o[0], o[1], rtol=RTOL)
-    # The same rays traced alone (a small call: the kernel keeps each lane's
-    # last cells, which a full-size call does not) give the same bits.
+    # The same rays traced alone (a small call) give the same bits; and
+    # repeated into a call of 78,720 rays, more blocks than one wave of the
+    # build that keeps each lane's last cells holds, so that call runs the
+    # build without that cache.
     del traj
     small = mr.trace(b, c, w.x0[idx], w.y0[idx], w.kx0[idx], w.ky0[idx], w.t_end - w.t0, w.dt,
                      t0=w.t0, math=MATH)
     assert np.array_equal(small.n_rows, rows1[idx])
     assert np.array_equal(np.nan_to_num(small.traj, nan=-1e300), np.nan_to_num(sub, nan=-1e300))
+    reps = 820
+    big_in = [torch.from_numpy(np.tile(a[idx], reps)).to(dev) for a in (w.x0, w.y0, w.kx0, w.ky0)]
+    nb = len(idx) * reps
+    big = torch.empty((5, rows, nb), dtype=torch.float64, device=dev)
+    nr_big = torch.empty(nb, dtype=torch.int32, device=dev)
+    st_big = torch.empty(nb, dtype=torch.uint8, device=dev)
+    mr.trace_device(b, c, *big_in, w.t0, w.t_end, w.dt, big, nr_big, st_big, math=MATH)
+    torch.cuda.synchronize()
+    for k in (0, reps - 1):
+        part = big[:, :, k * len(idx):(k + 1) * len(idx)].cpu().numpy()
+        assert np.array_equal(nr_big[k * len(idx):(k + 1) * len(idx)].cpu().numpy(), rows1[idx])
+        assert np.array_equal(np.nan_to_num(part, nan=-1e300), np.nan_to_num(sub, nan=-1e300))
 
 
 def test_vortex_field_and_shelf_bump(mr, oracle):
