@@ -59,8 +59,10 @@ ALG_FP32_FLOP_PER_RAY_STEP = 710.0
 # rays, 79.3 M ray-steps; sm__sass_thread_inst_executed_op_d{add,mul,fma}_pred_on).
 FP64_FLOP_PER_RAY_STEP = {"libm": 1399.1, "identity": 221.9}
 # FP64-pipe instructions per ray-step (sm__inst_executed_pipe_fp64 x 32: warp
-# instructions in lane slots, so lanes idle in a divergent warp count; same captures)
-FP64_PIPE_INST_PER_RAY_STEP = {"libm": 974.4, "identity": 223.4}
+# instructions in lane slots, so lanes idle in a divergent warp count; same
+# captures), of the build the 65,536-ray benchmark runs: identity with the
+# lookup cache, libm without (its cached build does not fit one wave)
+FP64_PIPE_INST_PER_RAY_STEP = {"libm": 974.4, "identity": 225.4}
 # DRAM bytes (read + written) per ray-step of the plain kernel on the seamount
 # workload: ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch
 # over its 65,536 rays x 1,000 steps (55.5 MB read, 2,573.7 MB written: the
