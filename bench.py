@@ -137,8 +137,9 @@ def parse():
     p.add_argument("--ns-calls", type=int, default=6,
                    help="shelf-slope: timed graph-replayed calls")
     p.add_argument("--ns-warmup", type=int, default=2, help="shelf-slope: untimed calls")
-    p.add_argument("--ns-plain-rays", type=int, default=262144,
-                   help="shelf-slope: rays of the plain FP64 form's rate measurement")
+    p.add_argument("--ns-plain-rays", type=int, default=1048576,
+                   help="shelf-slope: rays of the plain FP64 form's rate measurement (2^20: "
+                        "enough to fill the GPU as the rays end; 2^18 ran 13% slower)")
     p.add_argument("--ns-plain-chunk", type=int, default=2500,
                    help="shelf-slope: steps per plain FP64 launch (memory of full trajectories)")
     p.add_argument("--ns-error-rays", type=int, default=4096,
