@@ -162,3 +162,36 @@ def test_error_message_is_thread_local_and_set(native):
         read_netcdf3_variable("/nonexistent/file.nc", "x")
     assert b"nonexistent" in native.mr_last_error()
     _ = ctypes
+
+
+def test_batch_config_layout_matches_the_header(native, tmp_path):
+    # The ctypes mirror of mr_batch_config has the header's size and field
+    # offsets (a C program compiled against include/mantaray_gpu.h prints
+    # them), and the library's default config fills it as documented.
+    import shutil
+    import subprocess
+
+    from mantaray_gb300 import _native
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    fields = [f for f, _ in _native.BatchConfig._fields_]
+    src = tmp_path / "layout.c"
+    src.write_text(
+        "#include <stddef.h>\n#include <stdio.h>\n#include \"mantaray_gpu.h\"\n"
+        "int main(void) {\n"
+        "  printf(\"%zu\\n\", sizeof(mr_batch_config));\n"
+        + "".join(f"  printf(\"%zu\\n\", offsetof(mr_batch_config, {f}));\n" for f in fields)
+        + "  return 0;\n}\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                   check=True, capture_output=True)
+    out = [int(v) for v in subprocess.run([str(exe)], check=True, capture_output=True,
+                                          text=True).stdout.split()]
+    assert out[0] == ctypes.sizeof(_native.BatchConfig)
+    assert out[1:] == [getattr(_native.BatchConfig, f).offset for f in fields]
+    cfg = _native.BatchConfig()
+    assert native.mr_batch_default_config(ctypes.byref(cfg)) == 0
+    assert (cfg.block, cfg.blocks_per_sm, cfg.rays_per_lane, cfg.rebase_interval, cfg.order,
+            cfg.staging, cfg.sweep_steps) == (128, 4, 1, 32, 0, 0, 0)
