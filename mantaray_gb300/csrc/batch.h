@@ -30,7 +30,6 @@ struct PackedGrid {
   double x0, y0;         // first axis values
   double sp_x, sp_y;     // axis spacing (a[1] - a[0])
   float inv_sp_x, inv_sp_y;
-  float cx_max, cy_max;  // nx - 2, ny - 2: the last cell's index on each axis
   double inv_sp_xd, inv_sp_yd;  // 1 / spacing in FP64 (origin rebase)
   int kind;              // 0 grid, 1 constant (current only)
   float cu, cv;          // constant current

@@ -60,8 +60,6 @@ int pack_bathy(mr_batch *b, const mr_bathymetry *h, mr::PackedGrid *g, cudaStrea
   g->sp_y = h->dev.yspace;
   g->inv_sp_x = static_cast<float>(1.0 / h->dev.xspace);
   g->inv_sp_y = static_cast<float>(1.0 / h->dev.yspace);
-  g->cx_max = static_cast<float>(g->nx - 2);
-  g->cy_max = static_cast<float>(g->ny - 2);
   g->inv_sp_xd = 1.0 / h->dev.xspace;
   g->inv_sp_yd = 1.0 / h->dev.yspace;
   g->kind = 0;
@@ -78,7 +76,6 @@ int pack_current(mr_batch *b, const mr_current *c, mr::PackedGrid *g, cudaStream
     g->x0 = g->y0 = 0.0;
     g->sp_x = g->sp_y = 1.0;
     g->inv_sp_x = g->inv_sp_y = 1.0f;
-    g->cx_max = g->cy_max = 0.0f;
     g->inv_sp_xd = g->inv_sp_yd = 1.0;
     return MR_OK;
   }
@@ -101,8 +98,6 @@ int pack_current(mr_batch *b, const mr_current *c, mr::PackedGrid *g, cudaStream
   g->sp_y = c->dev.yspace;
   g->inv_sp_x = static_cast<float>(1.0 / c->dev.xspace);
   g->inv_sp_y = static_cast<float>(1.0 / c->dev.yspace);
-  g->cx_max = static_cast<float>(g->nx - 2);
-  g->cy_max = static_cast<float>(g->ny - 2);
   g->inv_sp_xd = 1.0 / c->dev.xspace;
   g->inv_sp_yd = 1.0 / c->dev.yspace;
   g->kind = 0;

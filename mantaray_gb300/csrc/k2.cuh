@@ -108,7 +108,13 @@ __device__ __forceinline__ bool locate(const PackedGrid &g, const GridPos &p, fl
                            static_cast<unsigned>(*ix));
   *fx = ux - flx;
   *fy = uy - fly;
-  return cx >= 0.0f && cx <= g.cx_max && cy >= 0.0f && cy <= g.cy_max;
+  // cx, cy are integral: for finite ones the unsigned test of their
+  // (saturated) conversions is the bounds test 0 <= cx <= nx - 2.  A NaN
+  // position converts to cell (0, 0) and passes it, but its fractions and
+  // so its depth are NaN: the stage fails all the same, with the same
+  // status (out of domain), and cell 0 is a valid load.
+  return static_cast<unsigned>(*ix) <= static_cast<unsigned>(g.nx - 2) &&
+         static_cast<unsigned>(*iy) <= static_cast<unsigned>(g.ny - 2);
 }
 
 __device__ __forceinline__ bool locate(const PackedGrid &g, const GridPos &p, float px, float py,
@@ -500,7 +506,10 @@ __device__ __forceinline__ int rhs_f32(const ScenarioDev &s, RayLane &L, const W
   const float h = bilin(C.b0, fx, fy);
   const float k2 = fmaf(kx, kx, ky * ky);
   ray_equations(h, u, v, dudx, dudy, dvdx, dvdy, C.bx, C.by, kx, ky, k2, d);
-  const bool wet = h > 0.0f, kok = k2 > 0.0f && k2 < 3.0e38f;
+  const bool wet = h > 0.0f;
+  // 0 < k2 < 3e38 on the bit pattern (k2 = kx^2 + ky^2 is +0, positive,
+  // +inf or NaN; 3e38 is 0x7f61b1e6): one integer compare
+  const bool kok = static_cast<unsigned>(__float_as_int(k2)) - 1u < 0x7f61b1e5u;
   if (!EXACT) return (inside && wet && kok) ? BATCH_COMPLETE : BATCH_OUT_OF_DOMAIN;
   if (inside && wet && kok) return BATCH_COMPLETE;
   if (!inside || (!(h <= 0.0f) && !wet)) return BATCH_OUT_OF_DOMAIN;
