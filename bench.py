@@ -63,14 +63,17 @@ FP64_FLOP_PER_RAY_STEP = {"libm": 1399.1, "identity": 221.9}
 # captures), of the build the 65,536-ray benchmark runs: identity with the
 # lookup cache, libm without (its cached build does not fit one wave)
 FP64_PIPE_INST_PER_RAY_STEP = {"libm": 974.4, "identity": 225.4}
-# DRAM bytes (read + written) per ray-step of the plain kernel on the seamount
-# workload: ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch
-# over its 65,536 rays x 1,000 steps (55.5 MB read, 2,573.7 MB written: the
-# 2.62 GB of stored rows, 20x L2, less what L2 still held at the end).
-K1_DRAM_BYTES_PER_RAY_STEP = (55537408 + 2573673472) / (65536 * 1000)
+# DRAM bytes (read + written) per stored trajectory row of the plain kernel
+# on the seamount workload: ncu dram__bytes_read.sum + dram__bytes_write.sum
+# of one launch over its 65,536 rays x 1,000 steps (55.5 MB read, 2,573.7 MB
+# written: the 2.62 GB of stored rows, 20x L2, less what L2 still held at the
+# end) over its 65,536 x 1,001 rows.  Scaled by rows (NaN padding included:
+# a ray that stops early still writes its padding rows), not ray-steps.
+K1_DRAM_BYTES_PER_ROW = (55537408 + 2573673472) / (65536 * 1001)
 K1_DRAM_NOTE = ("ncu DRAM bytes of a 65,536-ray x 1,000-step launch of the same workload "
-                "(55.5 MB read, 2,573.7 MB written) scaled by ray-steps; rows still in L2 at the "
-                "end of that launch (at most 129 MB) are not counted")
+                "(55.5 MB read, 2,573.7 MB written) scaled by stored rows (rays x rows, NaN "
+                "padding included); rows still in L2 at the end of that launch (at most 129 MB) "
+                "are not counted")
 # The same for the batched kernel on the shelf-slope field: one graph-replayed
 # call on the field's generator at 4,096^2 (records 1.3 GB, 10x L2) with the
 # 8,192^2 case's ray density, 5,466,581 rays traced to their ends (49.64 G
@@ -467,11 +470,11 @@ def gb300_arm(args, rank: int, world: int, local_rank: int):
                        "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"}
     # DRAM bytes of one launch: the algorithmic floor (the trajectory rows the
     # launch must store, NaN padding included) and the ncu count of a capture
-    # whose stored rows dwarf L2, scaled by ray-steps
+    # whose stored rows dwarf L2, scaled by stored rows
     must_store = 5 * 8 * rows * n + n * 5
     roofline["traffic_floor"] = must_store
-    if args.workload == "seamount" and K1_DRAM_BYTES_PER_RAY_STEP is not None:
-        roofline["traffic"] = K1_DRAM_BYTES_PER_RAY_STEP * ray_steps
+    if args.workload == "seamount":
+        roofline["traffic"] = K1_DRAM_BYTES_PER_ROW * rows * n
         roofline["traffic_note"] = K1_DRAM_NOTE
     else:
         roofline["traffic"] = None
