@@ -307,6 +307,19 @@ def test_page_locked_host_outputs_are_written_in_place(mr):
                      (host.saved, host.end_state, host.n_steps, host.n_saved, host.status)):
         np.testing.assert_array_equal(np.nan_to_num(a.cpu().numpy(), nan=-7.0),
                                       np.nan_to_num(b_.numpy(), nan=-7.0))
+    # the same in sweeps of 40 steps: rows written into host memory by
+    # several launches, the last states by the launch where each ray ends
+    from mantaray_gb300.batch import make_config
+
+    for t in (host.saved, host.end_state, host.n_steps, host.n_saved, host.status):
+        t.fill_(3)
+    tracer.trace(x0, y0, kx0, ky0, w.dt, 300, decimation=25, out=host,
+                 config=make_config(128, 4, 1, 32, 1, 0, 40))
+    torch.cuda.synchronize()
+    for a, b_ in zip((ref.saved, ref.end_state, ref.n_steps, ref.n_saved, ref.status),
+                     (host.saved, host.end_state, host.n_steps, host.n_saved, host.status)):
+        np.testing.assert_array_equal(np.nan_to_num(a.cpu().numpy(), nan=-7.0),
+                                      np.nan_to_num(b_.numpy(), nan=-7.0))
 
 
 def test_pageable_host_outputs_are_refused(mr):
@@ -722,6 +735,13 @@ def test_sweeps_across_scenarios(mr, same_grid):
                                  config=make_config(128, 4, 1, 32, 1, 0, sweep)))
         for x, y in zip(got, ref):
             np.testing.assert_array_equal(x, y)
+    # through a captured graph of the scenario-table build
+    g = tracer.graph(*ins, rays["dt"], 1500, decimation=100, scenario=sid,
+                     config=make_config(128, 4, 1, 32, 1, 0, 64))
+    g.launch()
+    for x, y in zip(_bits(g.out), ref):
+        np.testing.assert_array_equal(x, y)
+    g.close()
 
 
 def test_sweeps_refused_where_they_do_not_apply(mr):
