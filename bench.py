@@ -669,9 +669,11 @@ def north_star_batched(args, dev, stream, flush) -> dict:
         cfg = make_config(blk, bps, rpl, 32, order, *more[:2])
     else:
         # short probe of every shape on 2^20 rays, then the fastest six
-        # (and the ordered ones in sweeps) again on 2^22 rays over a long
-        # trace, where the rays have spread over the whole field
-        many = min(cap, 1 << 22)
+        # (and the ordered ones in sweeps) again on 2^23 rays over a long
+        # trace, where the rays have spread over the whole field (half the
+        # benchmark's ray density: how well sweeps share cell records
+        # depends on it)
+        many = min(cap, 1 << 23)
         cfg = tracer.autotune(*[t[:many] for t in ins], dt, min(steps, 1000), t0=t0,
                               cache_key=f"{torch.cuda.get_device_name(dev)}:{name}:{probe}:{many}",
                               long_steps=min(steps, 10000), long_rays=many, finalists=6,
