@@ -672,12 +672,13 @@ def north_star_batched(args, dev, stream, flush) -> dict:
         # (and the ordered ones in sweeps) again on 2^23 rays over a long
         # trace, where the rays have spread over the whole field (half the
         # benchmark's ray density: how well sweeps share cell records
-        # depends on it)
+        # depends on it), then the three fastest of those on the nominal
+        # call itself (16.8 M rays over the whole horizon, one call each)
         many = min(cap, 1 << 23)
-        cfg = tracer.autotune(*[t[:many] for t in ins], dt, min(steps, 1000), t0=t0,
+        cfg = tracer.autotune(*ins, dt, min(steps, 1000), t0=t0,
                               cache_key=f"{torch.cuda.get_device_name(dev)}:{name}:{probe}:{many}",
                               long_steps=min(steps, 10000), long_rays=many, finalists=6,
-                              probe_rays=probe)
+                              probe_rays=probe, final_rays=nominal, final_steps=steps)
     g = tracer.graph(*ins, dt, steps, t0=t0, config=cfg)
     out = g.out
     counts = np.random.default_rng(4004).integers(nominal // 2, cap + 1,

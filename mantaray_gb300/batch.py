@@ -137,8 +137,9 @@ class BatchTracer:
 
     def autotune(self, x0, y0, kx0, ky0, dt, probe_steps, t0=0.0, scenario=None,
                  candidates=None, repeats=2, cache_key=None, long_steps=None,
-                 long_rays=None, finalists=4, sweeps=(64, 96, 128),
-                 probe_rays=None) -> N.BatchConfig:
+                 long_rays=None, finalists=4, sweeps=(96, 128),
+                 probe_rays=None, final_rays=None, final_steps=None,
+                 final_count=3) -> N.BatchConfig:
         """Times every candidate launch shape on a probe run (the first
         `probe_rays` of the given rays, default all, for `probe_steps` steps,
         endpoints only) and returns the fastest.
@@ -146,10 +147,13 @@ class BatchTracer:
         first `long_rays` rays for `long_steps` steps, once each, and the
         fastest of that run wins: a short probe keeps the rays near their
         starts, where the fields they read may fit in L2, while a long trace
-        spreads them over the whole field.  There the two fastest ordered
+        spreads them over the whole field.  There the four fastest ordered
         one-ray finalists (or the fastest such candidate, if no finalist is
         one) are also timed in sweeps of each length in `sweeps`, a form that
-        only pays once the rays have spread.  Results are cached in memory and in
+        only pays once the rays have spread.  With `final_steps`, the
+        `final_count` fastest of that stage are timed once more on the first
+        `final_rays` rays for `final_steps` steps (the workload itself), and
+        the fastest there wins.  Results are cached in memory and in
         $MANTARAY_TUNE_CACHE (a JSON file) when that is set."""
         torch = _torch()
         key = cache_key
@@ -209,12 +213,21 @@ class BatchTracer:
                 return c.order == 1 and c.rays_per_lane == 1 and c.staging == 0 and \
                     c.sweep_steps == 0
 
-            bases = [c for c in finals if sweepable(c)][:2]
+            bases = [c for c in finals if sweepable(c)][:4]
             if not bases:
                 bases = [candidates[i] for _, i in ranked if sweepable(candidates[i])][:1]
             finals += [make_config(**dict(c.as_dict(), sweep_steps=sw))
                        for c in bases for sw in sweeps if 0 < sw < long_steps]
-            best = min(finals, key=lambda cfg: timed(cfg, rays, long_steps, 1, out))
+            ranked_long = sorted(((timed(cfg, rays, long_steps, 1, out), i)
+                                  for i, cfg in enumerate(finals)), key=lambda t: t[0])
+            best = finals[ranked_long[0][1]]
+            if final_steps:
+                f = int(min(x0.numel(), final_rays or x0.numel()))
+                rays = tuple(t[:f] for t in (x0, y0, kx0, ky0))
+                del out
+                out = self.alloc(f, final_steps, 0, device=x0.device)
+                last = [finals[i] for _, i in ranked_long[:final_count]]
+                best = min(last, key=lambda cfg: timed(cfg, rays, final_steps, 1, out))
         if key:
             _TUNE_CACHE[key] = best.as_dict()
             if cache_path:
