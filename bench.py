@@ -941,14 +941,16 @@ def batched_arm(args, rank: int, world: int, local_rank: int):
     elif not args.no_autotune:
         probe = min(n_all, 1 << 20)
         # long horizons: the fastest shapes (and the ordered ones in sweeps)
-        # again on 2^22 rays over 10,000 steps, where the rays have spread
-        many = min(n_all, 1 << 22) if steps >= 5000 else probe
-        pin = [t[:many] for t in ins]
-        cfg = tracer.autotune(*pin, dt, min(steps, 1000), t0=t0,
-                              scenario=sid[:many] if sid is not None else None,
+        # again on 2^22 rays over 10,000 steps, where the rays have spread,
+        # then the three fastest of those on the call itself
+        long_h = steps >= 5000
+        many = min(n_all, 1 << 22) if long_h else probe
+        cfg = tracer.autotune(*ins, dt, min(steps, 1000), t0=t0, scenario=sid,
                               cache_key=f"{torch.cuda.get_device_name(dev)}:{name}:{probe}:{many}",
-                              long_steps=min(steps, 10000) if steps >= 5000 else None,
-                              long_rays=many, finalists=6, probe_rays=probe)
+                              long_steps=min(steps, 10000) if long_h else None,
+                              long_rays=many, finalists=6, probe_rays=probe,
+                              final_rays=n_all if long_h else None,
+                              final_steps=steps if long_h else None)
         tuned = cfg.as_dict()
 
     rng = np.random.default_rng(7)
