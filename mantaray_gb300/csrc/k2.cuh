@@ -600,10 +600,10 @@ __device__ __forceinline__ void start(const BatchArgs &a, RayLane &L, int64_t r)
   }
 }
 
-// The sweep form: a ray taken up again from the state a previous launch left,
-// with no cell held -- exactly the lane of a launch
-// that traced it without stopping, as the cell records are a cache of
-// immutable values and the origin's grid positions a function of the origin.
+// The sweep form: a ray taken up again from the state a previous launch
+// left, with no cell held -- the lane a launch that traced it without
+// stopping would hold, as the cell records are a cache of immutable values
+// and the origin's grid positions a function of the origin.
 template <int MODE>
 __device__ __forceinline__ void resume(const BatchArgs &a, RayLane &L, int64_t r) {
   L.ray = r;
