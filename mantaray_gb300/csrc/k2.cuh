@@ -459,7 +459,8 @@ __device__ __forceinline__ void load_same_grid_cell_tile(const ScenarioDev &s, C
 // One right-hand side in FP32 at offset (px, py), wavenumber (kx, ky).
 // The fields come from the lane's cell records (loaded when the lane does not
 // hold the cell; a point outside a grid loads nothing and uses the records
-// held, whatever they are).  With EXACT, returns the stage's BatchStatus: out
+// held, whatever they are, and a NaN point reads cell 0's: its depth is NaN
+// all the same).  With EXACT, returns the stage's BatchStatus: out
 // of domain (outside a grid, or depth NaN: a cell past the depth array), dry
 // (depth <= 0), bad wavenumber (k^2 not in (0, 3e38)), else complete;
 // without, BATCH_COMPLETE or not (the same test, no status code).  d is
