@@ -546,6 +546,15 @@ def test_autotuner_long_stage_tries_sweeps(mr, monkeypatch):
     long_cfgs = [c for n, c in timed if n == 16384]
     assert dict(cands[1].as_dict(), sweep_steps=64) in long_cfgs  # 1000 > long_steps: not tried
     assert all(c["sweep_steps"] in (0, 64) for c in long_cfgs)
+    # a final stage: the two fastest of the long stage again on 8,192 rays
+    timed.clear()
+    monkeypatch.setattr(B, "_TUNE_CACHE", {})
+    cfg = tracer.autotune(*ins, w.dt, 100, candidates=cands, long_steps=400, long_rays=16384,
+                          finalists=2, sweeps=(64,), probe_rays=4096, final_rays=8192,
+                          final_steps=300, final_count=2)
+    finals = [c for n, c in timed if n == 8192]
+    assert len(finals) == 4  # two configurations, an untimed and a timed call each
+    assert cfg.as_dict() in finals
 
 
 def test_decimation_tuner_budgets(mr):
