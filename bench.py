@@ -82,7 +82,7 @@ K1_DRAM_NOTE = ("ncu DRAM bytes of a 65,536-ray x 1,000-step launch of the same 
 # rays' states written and read between sweeps).  Its rays spread over the
 # field as the 8,192^2 case's do, so the bytes scale with ray-steps.
 K2_SHELF_RAY_STEPS = 49640953115
-K2_SHELF_DRAM_BYTES = {0: (1690693872640, 1447764224), 128: (103553328384, 28901769472),
+K2_SHELF_DRAM_BYTES = {0: (1690693872640, 1447764224), 128: (98504049152, 28714596608),
                        256: (61612061696, 15217717760)}
 
 
