@@ -6,8 +6,11 @@
 // K2 (rk4_f32_kernel_1 / _1r / _2, device code in k2.cuh): a persistent
 // kernel, grid = SMs x blocks per SM.  Each lane holds 1 or 2 rays (_2); one
 // ray per lane has an uncapped and a 72-register build (_1r), chosen by the
-// launch shape.  Each build has two scenario-table forms (instantiated here)
-// and two single-scenario forms (rk4_f32_one.cu).  A lane whose ray has ended
+// launch shape, and their sweep forms (_1s / _1rs: each launch advances its
+// rays by at most sweep_steps steps, the rays still running re-sorted by
+// position between launches; batch_api.cu queues the sequence).  Each build
+// has two scenario-table forms (instantiated here) and two single-scenario
+// forms (rk4_f32_one.cu).  A lane whose ray has ended
 // refills from a device work queue: the warp ballots its empty slots, one lane reserves
 // that many ray indices with a single atomicAdd and the indices are handed out
 // by rank within the ballot, so lanes never idle while work remains and rays
